@@ -1,0 +1,173 @@
+/*
+ * spintrack.h — C ABI of the GB300-native spin-tracking engine (sm_103a).
+ *
+ * Drop-in for the per-particle hot path of rtat-caltech/Spin-tracking: the
+ * params.txt options, the particle engine (init / run to the next output time
+ * / read the snapshot), the window driver, and binary output format 'A'.
+ * Citations name the reference interface each entry point replaces
+ * (paths relative to the reference repository root).
+ *
+ * Conventions: plain C types only; every call returns 0 (ST_OK) or a negative
+ * ST_ERR_* code and never exits the process (the reference's gpuErrchk calls
+ * exit(), include/particle.h:23-32); st_last_error() describes the most recent
+ * failure of the calling thread.  A context is single-threaded: one host
+ * thread, one CUDA stream, one device.
+ */
+#ifndef SPINTRACK_H
+#define SPINTRACK_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ST_OK 0
+#define ST_ERR_ARG (-1)         /* bad argument or option value */
+#define ST_ERR_CUDA (-2)        /* CUDA runtime error (message in st_last_error) */
+#define ST_ERR_UNSUPPORTED (-3) /* option outside the implemented path (e.g. integratorType 2-6) */
+#define ST_ERR_IO (-4)          /* file could not be opened or written */
+#define ST_ERR_STATE (-5)       /* call out of order (e.g. run before init) */
+#define ST_ERR_DEADLINE (-6)    /* device time budget ran out; state is saved and resumable */
+#define ST_ERR_NOMEM (-7)       /* allocation failed */
+
+typedef struct st_vec3 { double x, y, z; } st_vec3;
+
+/* Field-for-field the reference's `struct options` (include/options.h:10-61),
+ * same order, types and defaults: 440 bytes on LP64.  Its byte image is the
+ * header of output format 'A' (src/logger.cpp:27-29). */
+typedef struct st_options {
+  st_vec3 B0, E, L, yi, Gx, Gy, Gz;
+  double m, t0, tf, rtol, atol, beta, uround, safe, fac1, fac2, hmax, hmin, h, T;
+  double sqrtKT_m, tc, gamma, V, a, w, swapStepSize, maxPosStep, ioutInt, diffuse;
+  unsigned int nmax, seed;
+  int integratorType, numParticles, numPerGPUBlock, iout;
+  char dist;
+  bool gas_coll, gravity, fixedStepSize, keepStepSize;
+  st_vec3 noiseAmplitudes, noiseFrequencies;
+} st_options;
+
+/* Host (or device) arrays of numParticles entries each, one per snapshot field
+ * of format 'A' (src/logger.cpp:14-25).  A NULL member is skipped. */
+typedef struct st_state_view {
+  double *t;
+  st_vec3 *pos, *v, *S;
+  int32_t *fail;
+  uint64_t *n_coll, *n_bounce, *n_steps;
+} st_state_view;
+
+/* Device-resident particle state, structure of arrays (borrowed pointers,
+ * valid until st_destroy).  Component arrays of length n_total. */
+typedef struct st_device_soa {
+  int64_t n_total;
+  double *t, *pos_x, *pos_y, *pos_z, *v_x, *v_y, *v_z, *S_x, *S_y, *S_z, *h, *next_gas;
+  int32_t *fail;
+  uint64_t *n_coll, *n_bounce, *n_steps;
+  uint8_t *stop;
+} st_device_soa;
+
+/* Which kernel advances the particles. */
+#define ST_KERNEL_PLAIN 0      /* one thread per particle, one launch per output window */
+#define ST_KERNEL_PERSISTENT 1 /* persistent work-queue kernel, lanes refilled as particles finish */
+
+/* Launch configuration of the persistent kernel (autotuned when zero). */
+typedef struct st_launch_config {
+  int block_threads;   /* threads per block; 0 = autotune */
+  int blocks_per_sm;   /* resident blocks per SM; 0 = autotune */
+  int variant;         /* kernel variant index (register budget); -1 = autotune */
+} st_launch_config;
+
+/* ---- library ---------------------------------------------------------- */
+int st_version(void);
+const char *st_last_error(void);
+
+/* ---- options (include/options.h, src/optionsParser.cpp) ---------------- */
+size_t st_options_size(void);
+/* options{} default member values, include/options.h:10-61 */
+void st_options_default(st_options *opt);
+/* parseLine, src/optionsParser.cpp:40-175.  Returns 0 when the key was
+ * applied, 1 for an unrecognised key (ignored, as the reference does),
+ * ST_ERR_ARG for a line with fewer than two fields or a malformed number. */
+int st_parse_line(st_options *opt, const char *line);
+/* optionParser, src/optionsParser.cpp:177-197: defaults, then every line of
+ * the file.  A missing file leaves the defaults (as the reference does) and
+ * returns ST_ERR_IO so the caller can tell. */
+int st_parse_params(const char *path, st_options *opt);
+/* Derived parameters of mainAnalysis, src/simulation.cpp:9-11:
+ * tc = 1.6e-4 m / (k T^8), sqrtKT_m = sqrt(k T / m). */
+void st_derive(st_options *opt);
+/* Number of output windows of a run: floor((tf - t0) / ioutInt),
+ * src/simulation.cpp:43. */
+int st_num_windows(const st_options *opt);
+
+/* ---- engine: class particle (include/particle.h:87-314) --------------- */
+typedef struct st_ctx st_ctx;
+/* particle::particle(options), include/particle.h:90-166: allocates the
+ * device state for opt->numParticles particles (taken as given: call
+ * st_derive first, as mainAnalysis does). */
+int st_create(const st_options *opt, int device, st_ctx **out);
+/* Batched form: nsets parameter sets, set s holding sets[s].numParticles
+ * particles seeded exactly as an independent reference run with sets[s]. */
+int st_create_batch(const st_options *sets, int nsets, int device, st_ctx **out);
+/* particle::~particle, include/particle.h:167-240 */
+void st_destroy(st_ctx *ctx);
+/* particle::initParticles, include/particle.h:241-252 (initParticlesCPU
+ * semantics, src/particle.cpp:638-710). */
+int st_init(st_ctx *ctx);
+/* particle::runSimulation(nextTOut), src/particle.cpp:865-876: advance every
+ * particle to next_t with the plain kernel (one launch). */
+int st_run_until(st_ctx *ctx, double next_t);
+/* Window loop of mainAnalysis, src/simulation.cpp:43-61: advance windows
+ * [w_begin, w_end) (window i ends at (i+1)*ioutInt), clamped per set to its
+ * own window count.  If snap != NULL, the state at the end of each window is
+ * written to it: (w_end - w_begin) consecutive blocks, each laid out as
+ * st_snapshot_bytes(ctx) bytes (see st_snapshot_field_offset).  snap is a
+ * device pointer. */
+int st_run_windows(st_ctx *ctx, int kernel, int w_begin, int w_end, void *snap);
+/* Bytes of one device snapshot block and the offset of field f within it
+ * (f: 0 t, 1 pos_x, 2 pos_y, 3 pos_z, 4 v_x, 5 v_y, 6 v_z, 7 S_x, 8 S_y,
+ * 9 S_z, 10 fail(i32), 11 n_coll, 12 n_bounce, 13 n_steps; each field an
+ * array over all particles, 256-byte aligned). */
+size_t st_snapshot_bytes(const st_ctx *ctx);
+size_t st_snapshot_field_offset(const st_ctx *ctx, int field);
+/* particle::outputData, src/particle.cpp:852-862: synchronise and copy the
+ * eight snapshot fields of every particle to host arrays. */
+int st_read_state(st_ctx *ctx, const st_state_view *host);
+/* Borrowed device pointers to the SoA state. */
+int st_device_state(st_ctx *ctx, st_device_soa *out);
+int st_synchronize(st_ctx *ctx);
+/* Persistent-kernel launch configuration (NULL = autotune on first use). */
+int st_set_launch_config(st_ctx *ctx, const st_launch_config *cfg);
+int st_get_launch_config(const st_ctx *ctx, st_launch_config *cfg);
+/* Device time budget for each following run call, in seconds (0 = none).
+ * When it runs out, kernels save the particle state and the call returns
+ * ST_ERR_DEADLINE; calling again resumes. */
+int st_set_deadline(st_ctx *ctx, double seconds);
+/* Work counters of the last run call: DOP853 and RK45 step attempts,
+ * trajectory segments, and kernels launched. */
+typedef struct st_counters {
+  uint64_t dop_attempts, rk45_attempts, segments, kernel_launches;
+} st_counters;
+int st_get_counters(const st_ctx *ctx, st_counters *out);
+
+/* FP64 FMA issue-rate probe (TFLOP/s, FMA = 2 flops): eight independent
+ * DFMA chains per thread on every SM.  No counterpart in the reference; it is
+ * the roofline denominator for the step kernels, which are FP64-pipe bound. */
+int st_probe_fp64_peak(int device, double *tflops);
+
+/* ---- driver: mainAnalysis (src/simulation.cpp:8-96) -------------------- */
+/* Derive tc/sqrtKT_m, create, init, write the options header and the t0
+ * snapshot, run every window with `kernel`, append a snapshot per window
+ * (format 'A', src/logger.cpp:14-38).  run_seconds (may be NULL) receives the
+ * wall time of the window loop excluding file writes. */
+int st_main_analysis(const st_options *opt, const char *out_path, int device, int kernel, double *run_seconds);
+/* Format 'A' writer pieces, for callers that hold their own state. */
+int st_write_header(void *file /* FILE* */, const st_options *opt);
+int st_write_snapshot(void *file /* FILE* */, int n, const st_state_view *host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,137 @@
+// Probe driver that calls the reference's own hot-path functions directly and
+// prints their results as C99 hex floats, one value per token.  Test
+// infrastructure only: it is compiled against the reference sources by
+// `make -C oracle ref` and used by tests/golden/make_golden.py to generate the
+// committed golden vectors.  Nothing in the product links it.
+//
+// Commands (all options come from a reference params file, parsed by the
+// reference's own optionParser, src/optionsParser.cpp:177):
+//   ref_probe init   PARAMS          initParticlesCPU (src/particle.cpp:638) for
+//                                     numParticles particles; prints per particle
+//                                     pos, v, next_gas_coll_time, rng x y z w
+//   ref_probe draws  PARAMS K        per particle after init: K raw xoshiro
+//                                     outputs (src/particle.cpp:59), then K
+//                                     normal(0,1) draws (src/particle.cpp:89)
+//   ref_probe dop    PARAMS t0 tf y0x y0y y0z px py pz vx vy vz h
+//   ref_probe rk45   PARAMS ...same...  integrateDOP / integrateRK45
+//                                     (src/integrator.cpp:90, :251) over one
+//                                     ballistic segment from (p, v) at t0;
+//                                     prints ret, y, h
+//   ref_probe events PARAMS NSEG      per particle after init: NSEG rounds of
+//                                     calc_next_collision_time + update +
+//                                     sanity_check (src/particle.cpp:121-444)
+//                                     with tf = opt.tf; prints per segment
+//                                     coll_type wall_hit dt t pos v next_gas
+#include "include/particle.h"
+#include "include/optionsParser.h"
+#include "include/integrator.h"
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+#include <cstring>
+
+static void hx(double x) { std::printf(" %a", x); }
+
+static options load(const char* path) {
+  options opt = optionParser(const_cast<char*>(path));
+  const double k = 1.380649e-23;  // same derivation as src/simulation.cpp:9-11
+  opt.tc = 1.6e-4 * opt.m / (k * pow(opt.T, 8.0));
+  opt.sqrtKT_m = sqrt(k * opt.T / opt.m);
+  return opt;
+}
+
+struct Arrays {
+  int n;
+  std::vector<coords> S, v, v_old, pos, pos_old;
+  std::vector<double> t, t_old, tf, dt, next_gas, h;
+  std::vector<rngState> state;
+  std::vector<size_t> n_bounce, n_coll, n_steps;
+  std::vector<unsigned int> partID;
+  std::vector<int> fail;
+  std::vector<bool> stop_unused;
+  bool* stop;
+  std::vector<char> coll_type, wall_hit;
+  SpectrumAggregator* spec;
+  explicit Arrays(int n_) : n(n_), S(n), v(n), v_old(n), pos(n), pos_old(n), t(n), t_old(n), tf(n),
+      dt(n), next_gas(n), h(n), state(n), n_bounce(n), n_coll(n), n_steps(n), partID(n), fail(n),
+      coll_type(n), wall_hit(n) {
+    stop = new bool[n];
+    spec = new SpectrumAggregator[n];
+  }
+};
+
+static void init_all(const options& opt, Arrays& a) {
+  floquetDiagonalization fd{};
+  initParticlesCPU(opt, a.S.data(), a.v.data(), a.v_old.data(), a.pos.data(), a.pos_old.data(),
+                   a.t.data(), a.t_old.data(), a.tf.data(), a.dt.data(), a.next_gas.data(), a.h.data(),
+                   a.state.data(), a.n_bounce.data(), a.n_coll.data(), a.n_steps.data(), a.partID.data(),
+                   a.fail.data(), a.stop, a.coll_type.data(), a.wall_hit.data(), a.spec, fd);
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) { std::fprintf(stderr, "usage: ref_probe CMD PARAMS ...\n"); return 2; }
+  const char* cmd = argv[1];
+  options opt = load(argv[2]);
+  if (!std::strcmp(cmd, "init") || !std::strcmp(cmd, "draws") || !std::strcmp(cmd, "events")) {
+    Arrays a(opt.numParticles);
+    init_all(opt, a);
+    for (int i = 0; i < a.n; ++i) {
+      std::printf("p %d", i);
+      if (!std::strcmp(cmd, "init")) {
+        hx(a.pos[i].x); hx(a.pos[i].y); hx(a.pos[i].z);
+        hx(a.v[i].x); hx(a.v[i].y); hx(a.v[i].z);
+        hx(a.next_gas[i]);
+        std::printf(" %llu %llu %llu %llu %d", (unsigned long long)a.state[i].x, (unsigned long long)a.state[i].y,
+                    (unsigned long long)a.state[i].z, (unsigned long long)a.state[i].w, (int)a.state[i].hasSpare);
+        hx(a.state[i].hasSpare ? a.state[i].spare : 0.0);
+        std::printf("\n");
+      } else if (!std::strcmp(cmd, "draws")) {
+        int k = std::atoi(argv[3]);
+        rngState s = a.state[i];
+        for (int j = 0; j < k; ++j) std::printf(" %llu", (unsigned long long)xoshiro256p(s));
+        for (int j = 0; j < k; ++j) hx(normal(s, 0.0, 1.0));
+        std::printf("\n");
+      } else {
+        int nseg = std::atoi(argv[3]);
+        double t = a.t[i], t_old = a.t_old[i], ng = a.next_gas[i], dt = 0.0;
+        coords pos = a.pos[i], pos_old = a.pos_old[i], v = a.v[i], v_old = a.v_old[i];
+        rngState s = a.state[i];
+        size_t nb = 0, nc = 0;
+        char ct = 'W', wh = 0;
+        bool fin = false, stop = false;
+        int fail = 0;
+        std::printf("\n");
+        for (int j = 0; j < nseg && !fin && !stop; ++j) {
+          calc_next_collision_time(t, opt.tf, v, pos, ng, dt, ct, nb, nc, fin, wh, s, opt);
+          update_position_and_velocity(t_old, t, dt, pos_old, pos, v_old, v, ct, wh, s, stop, opt);
+          sanity_check(t_old, t, pos_old, pos, v, v_old, ct, wh, stop, fail, opt);
+          std::printf("s %c %c %d %d", ct, wh ? wh : '-', (int)stop, fail);
+          hx(dt); hx(t); hx(pos.x); hx(pos.y); hx(pos.z); hx(v.x); hx(v.y); hx(v.z); hx(ng);
+          std::printf(" %llu\n", (unsigned long long)s.x);
+        }
+      }
+    }
+    return 0;
+  }
+  if (!std::strcmp(cmd, "dop") || !std::strcmp(cmd, "rk45")) {
+    if (argc < 16) { std::fprintf(stderr, "dop/rk45 need 13 numbers\n"); return 2; }
+    double vals[13];
+    for (int j = 0; j < 13; ++j) vals[j] = std::strtod(argv[3 + j], nullptr);
+    double t0 = vals[0], tf = vals[1];
+    coords y = {vals[2], vals[3], vals[4]};
+    coords p = {vals[5], vals[6], vals[7]};
+    coords v = {vals[8], vals[9], vals[10]};
+    double h = vals[11];
+    (void)vals[12];
+    // end-of-segment state is only used by the reference for signature parity
+    coords p_new = p, v_new = v;
+    int ret = !std::strcmp(cmd, "dop") ? integrateDOP(t0, tf, y, p, p_new, v, v_new, opt, h)
+                                      : integrateRK45(t0, tf, y, p, p_new, v, v_new, opt, h);
+    std::printf("r %d", ret);
+    hx(y.x); hx(y.y); hx(y.z); hx(h);
+    std::printf("\n");
+    return 0;
+  }
+  std::fprintf(stderr, "unknown command %s\n", cmd);
+  return 2;
+}

@@ -1,0 +1,111 @@
+/*
+ * ORACLE — test infrastructure only.  A plain-C restatement of the reference
+ * Spin-tracking hot path (rtat-caltech/Spin-tracking), used by tests/ as the
+ * parity checker and by bench.py as the timed CPU baseline.  The product
+ * (spin-tracking_gb300/) never links, loads or calls anything here.
+ *
+ * Every floating-point expression keeps the reference's evaluation order so
+ * that, compiled with -ffp-contract=off, results are bit-identical to the
+ * reference CPU build on the same host (checked against golden vectors made by
+ * the reference itself, tests/golden/).
+ */
+#ifndef SPIN_ORACLE_H
+#define SPIN_ORACLE_H
+
+#include <stdint.h>
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { double x, y, z; } or_vec3;
+
+/* Field-for-field image of the reference's `struct options`
+ * (include/options.h:10-61): 440 bytes on LP64, also the format-'A' header. */
+typedef struct {
+  or_vec3 B0, E, L, yi, Gx, Gy, Gz;
+  double m, t0, tf, rtol, atol, beta, uround, safe, fac1, fac2, hmax, hmin, h, T;
+  double sqrtKT_m, tc, gamma, V, a, w, swapStepSize, maxPosStep, ioutInt, diffuse;
+  unsigned int nmax, seed;
+  int integratorType, numParticles, numPerGPUBlock, iout;
+  char dist;
+  bool gas_coll, gravity, fixedStepSize, keepStepSize;
+  or_vec3 noiseAmplitudes, noiseFrequencies;
+} or_options;
+
+/* Reference rngState (include/particle.h:52-59). */
+typedef struct {
+  uint64_t x, y, z, w;
+  double spare;
+  bool has_spare;
+} or_rng;
+
+/* Per-particle state, structure of arrays, owned by the caller. */
+typedef struct {
+  int n;
+  or_vec3 *S, *v, *v_old, *pos, *pos_old;
+  double *t, *t_old, *h, *next_gas;
+  or_rng *rng;
+  int *fail;
+  uint64_t *n_bounce, *n_coll, *n_steps;
+  bool *stop;
+  char *coll_type, *wall_hit;
+} or_particles;
+
+size_t or_options_size(void);
+void or_options_default(or_options *opt);
+/* parseLine (src/optionsParser.cpp:40-175); returns 0 if the key was used. */
+int or_parse_line(or_options *opt, const char *line);
+/* optionParser (src/optionsParser.cpp:177-197); missing file = defaults. */
+int or_parse_file(const char *path, or_options *opt);
+/* tc and sqrtKT_m as mainAnalysis derives them (src/simulation.cpp:9-11). */
+void or_derive(or_options *opt);
+
+/* RNG (src/particle.cpp:33-119). */
+void or_rng_seed(or_rng *r, unsigned int seed, unsigned int ipart);
+uint64_t or_xoshiro(or_rng *r);
+double or_uniform(or_rng *r);
+double or_normal(or_rng *r, double mean, double std);
+double or_exponential(or_rng *r, double tc);
+
+/* Particle engine (src/particle.cpp:638-825). */
+int or_particles_alloc(or_particles *p, int n);
+void or_particles_free(or_particles *p);
+void or_init(const or_options *opt, or_particles *p, int first_index);
+void or_run_until(const or_options *opt, or_particles *p, double next_t, int nthreads);
+
+/* Steppers over one ballistic segment (src/integrator.cpp:90-337). */
+int or_integrate_dop(const or_options *opt, double t0, double tf, or_vec3 *y, const or_vec3 *p_old,
+                     const or_vec3 *v_old, double *h);
+int or_integrate_rk45(const or_options *opt, double t0, double tf, or_vec3 *y, const or_vec3 *p_old,
+                      const or_vec3 *v_old, double *h);
+
+/* Ballistic interpolation (src/integrator.cpp:48-61). */
+void or_interpolate(const or_options *opt, double t, double t0, const or_vec3 *p_old, const or_vec3 *v_old,
+                    or_vec3 *p_out, or_vec3 *v_out);
+
+/* One segment event: calc_next_collision_time + update_position_and_velocity
+ * + sanity_check (src/particle.cpp:121-444) for particle i with window end tf.
+ * Returns the `finished` flag. */
+int or_event(const or_options *opt, or_particles *p, int i, double tf);
+
+/* mainAnalysis (src/simulation.cpp:8-96) writing format 'A' to out_path.
+ * opt is taken as given (call or_derive first, as the reference does).
+ * Returns 0 on success; *run_seconds receives the summed window time. */
+int or_main_analysis(const or_options *opt, const char *out_path, int nthreads, double *run_seconds);
+
+/* Bounded CPU baseline: particles [first, first+count) of opt's run, all
+ * windows, no file output.  Returns the wall seconds spent. */
+double or_run_sample(const or_options *opt, int first, int count, int nthreads, or_particles *out);
+
+/* Instrumented count of DOP853 step attempts and segments, for the roofline
+ * work model: filled by or_run_until when non-null. */
+typedef struct { uint64_t dop_attempts, rk45_attempts, segments; } or_counters;
+void or_set_counters(or_counters *c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

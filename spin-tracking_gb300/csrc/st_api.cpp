@@ -1,0 +1,854 @@
+// Host library behind include/spintrack.h: options parsing, the engine
+// context (device state, parameter-set table, stream), the window driver and
+// the format-'A' writer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spintrack.h"
+#include "st_internal.h"
+
+using st::SetParams;
+
+static_assert(sizeof(st_options) == 440, "st_options must match the reference options image");
+static_assert(sizeof(st_vec3) == 24, "st_vec3 layout");
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define ST_CUDA(expr)                                                                            \
+  do {                                                                                           \
+    cudaError_t e_ = (expr);                                                                     \
+    if (e_ != cudaSuccess) return fail(ST_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define ST_TRY(expr)            \
+  do {                          \
+    int r_ = (expr);            \
+    if (r_ != ST_OK) return r_; \
+  } while (0)
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------- parsing
+std::vector<std::string> split_fields(const char* line) {
+  // grabElementsInLine + removeWhitespace (src/optionsParser.cpp:11-37)
+  std::vector<std::string> out(1);
+  for (const char* c = line; *c; ++c) {
+    if (*c == ',')
+      out.emplace_back();
+    else if (!std::isspace(static_cast<unsigned char>(*c)))
+      out.back().push_back(*c);
+  }
+  return out;
+}
+
+bool to_double(const std::string& s, double* v) {
+  if (s.empty()) return false;
+  char* end = nullptr;
+  errno = 0;
+  const double x = std::strtod(s.c_str(), &end);
+  if (end == s.c_str()) return false;  // no conversion: leave the option unchanged
+  *v = x;
+  return true;
+}
+
+bool to_int(const std::string& s, int* v) {
+  if (s.empty()) return false;
+  char* end = nullptr;
+  errno = 0;
+  long x = std::strtol(s.c_str(), &end, 10);
+  if (end == s.c_str() || errno == ERANGE || x > 2147483647L || x < -2147483648L) return false;
+  *v = (int)x;
+  return true;
+}
+
+// to_bool (src/optionsParser.cpp:16-22): boolalpha extraction of the lowered
+// token, so a leading "true" gives true and anything else false.
+bool to_bool(const std::string& s) {
+  std::string low;
+  for (char c : s) low.push_back((char)std::tolower(static_cast<unsigned char>(c)));
+  return low.compare(0, 4, "true") == 0;
+}
+
+// ---------------------------------------------------------------- params
+int build_params(const st_options& o, int64_t first, SetParams* P) {
+  if (o.numParticles < 0) return fail(ST_ERR_ARG, "numParticles must be >= 0");
+  if (o.integratorType >= 2 && o.integratorType <= 6)
+    return fail(ST_ERR_UNSUPPORTED, "integratorType " + std::to_string(o.integratorType) +
+                                        " (RKF45 / quaternion / Magnus / spectrum) is not implemented; use 0 (DOP853) or 1 (RK45)");
+  if (o.dist != 'C' && o.dist != 'M')
+    return fail(ST_ERR_UNSUPPORTED, std::string("dist must be 'C' or 'M', got '") + o.dist + "'");
+  if (!(o.ioutInt > 0.0)) return fail(ST_ERR_ARG, "ioutInt must be > 0");
+  std::memset(P, 0, sizeof(*P));
+  P->Lx = o.L.x; P->Ly = o.L.y; P->Lz = o.L.z;
+  P->maxPosStep = o.maxPosStep;
+  P->tc = o.tc;
+  P->sqrtKT_m = o.sqrtKT_m;
+  P->diffuse = o.diffuse;
+  P->V = o.V;
+  P->gamma = o.gamma;
+  P->B0x = o.B0.x; P->B0y = o.B0.y; P->B0z = o.B0.z;
+  P->Ex = o.E.x; P->Ey = o.E.y; P->Ez = o.E.z;
+  P->Gx[0] = o.Gx.x; P->Gx[1] = o.Gx.y; P->Gx[2] = o.Gx.z;
+  P->Gy[0] = o.Gy.x; P->Gy[1] = o.Gy.y; P->Gy[2] = o.Gy.z;
+  P->Gz[0] = o.Gz.x; P->Gz[1] = o.Gz.y; P->Gz[2] = o.Gz.z;
+  P->a = o.a;
+  P->w = o.w;
+  P->inv_c2 = 1.0 / st::kC2;
+  P->rtol = o.rtol; P->atol = o.atol; P->hmin = o.hmin; P->hmax = o.hmax; P->h0 = o.h;
+  P->safe = o.safe; P->fac1 = o.fac1; P->fac2 = o.fac2; P->beta = o.beta;
+  P->facc1 = 1.0 / o.fac1;
+  P->facc2 = 1.0 / o.fac2;
+  P->expo1 = 1.0 / 8.0 - o.beta * 0.2;
+  P->inv_safe = 1.0 / o.safe;
+  P->t0 = o.t0; P->tf = o.tf; P->ioutInt = o.ioutInt;
+  P->yi_x = o.yi.x; P->yi_y = o.yi.y; P->yi_z = o.yi.z;
+  P->nmax = o.nmax;
+  P->seed = o.seed;
+  P->integrator = o.integratorType;
+  P->nwin = st_num_windows(&o);
+  P->gravity = o.gravity ? 1 : 0;
+  P->gas = o.gas_coll ? 1 : 0;
+  P->fixed = o.fixedStepSize ? 1 : 0;
+  P->keep = o.keepStepSize ? 1 : 0;
+  P->dist = o.dist;
+  P->first = first;
+  P->n = o.numParticles;
+  return ST_OK;
+}
+
+}  // namespace
+
+// ==================================================================== context
+struct st_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<st_options> opts;
+  std::vector<SetParams> sets_h;
+  SetParams* sets_d = nullptr;
+  int64_t n = 0;
+  st::DeviceState s{};
+  void* arena = nullptr;
+  st::RunStatus* status_d = nullptr;
+  st::RunStatus* status_h = nullptr;  // pinned
+  int64_t* order_d = nullptr;
+  bool initialized = false;
+  bool window_grid = true;  // particles sit on window boundaries (false after st_run_until off-grid)
+  st_launch_config lc{0, 0, -1};
+  int sm_count = 0;
+  double deadline_s = 0.0;
+  st_counters last{};
+  st::SnapLayout snap{};
+};
+
+namespace {
+
+int ctx_alloc(st_ctx* c) {
+  const int64_t n = c->n;
+  const size_t m = (size_t)std::max<int64_t>(n, 1);
+  // one arena for every per-particle array, each 256-byte aligned
+  struct Field {
+    void** ptr;
+    size_t elem;
+  };
+  st::DeviceState& s = c->s;
+  Field f[] = {{(void**)&s.t, 8},        {(void**)&s.px, 8},   {(void**)&s.py, 8},     {(void**)&s.pz, 8},
+               {(void**)&s.vx, 8},       {(void**)&s.vy, 8},   {(void**)&s.vz, 8},     {(void**)&s.Sx, 8},
+               {(void**)&s.Sy, 8},       {(void**)&s.Sz, 8},   {(void**)&s.h, 8},      {(void**)&s.next_gas, 8},
+               {(void**)&s.rx, 8},       {(void**)&s.ry, 8},   {(void**)&s.rz, 8},     {(void**)&s.rw, 8},
+               {(void**)&s.rspare, 8},   {(void**)&s.rhas, 1}, {(void**)&s.fail, 4},   {(void**)&s.n_coll, 8},
+               {(void**)&s.n_bounce, 8}, {(void**)&s.n_steps, 8}, {(void**)&s.stop, 1}, {(void**)&s.coll, 1},
+               {(void**)&s.wall, 1},     {(void**)&s.set, 4},  {(void**)&s.w_done, 4}};
+  size_t total = 0;
+  for (auto& x : f) total += align256(x.elem * m);
+  cudaError_t e = cudaMalloc(&c->arena, total);
+  if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("cudaMalloc state: ") + cudaGetErrorString(e));
+  char* p = (char*)c->arena;
+  for (auto& x : f) {
+    *x.ptr = p;
+    p += align256(x.elem * m);
+  }
+  s.n = n;
+  ST_CUDA(cudaMemsetAsync(c->arena, 0, total, c->stream));
+  // set index of every particle
+  std::vector<int32_t> set_of((size_t)m, 0);
+  for (size_t k = 0; k < c->sets_h.size(); ++k)
+    for (int64_t j = 0; j < c->sets_h[k].n; ++j) set_of[(size_t)(c->sets_h[k].first + j)] = (int32_t)k;
+  ST_CUDA(cudaMemcpyAsync(s.set, set_of.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  ST_CUDA(cudaMalloc(&c->sets_d, sizeof(SetParams) * std::max<size_t>(c->sets_h.size(), 1)));
+  ST_CUDA(cudaMemcpyAsync(c->sets_d, c->sets_h.data(), sizeof(SetParams) * c->sets_h.size(), cudaMemcpyHostToDevice,
+                          c->stream));
+  ST_CUDA(cudaMalloc(&c->status_d, sizeof(st::RunStatus)));
+  ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
+  ST_CUDA(cudaMallocHost(&c->status_h, sizeof(st::RunStatus)));
+  // snapshot block layout: 14 arrays of n entries
+  const size_t esz[14] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 4, 8, 8, 8};
+  size_t off = 0;
+  c->snap.n = n;
+  for (int k = 0; k < 14; ++k) {
+    c->snap.off[k] = off;
+    off += align256(esz[k] * m);
+  }
+  c->snap.bytes = off;
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  return ST_OK;
+}
+
+// Work order for the persistent queue: longest expected particles first
+// (RK45 sets, then by simulated time), so the tail of the run is short.
+int ctx_build_order(st_ctx* c) {
+  if (c->order_d || c->sets_h.size() <= 1) return ST_OK;
+  std::vector<int> idx(c->sets_h.size());
+  for (size_t k = 0; k < idx.size(); ++k) idx[k] = (int)k;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+    const SetParams &A = c->sets_h[a], &B = c->sets_h[b];
+    const double ca = (A.integrator == 1 ? 1000.0 : 1.0) * A.nwin * A.ioutInt;
+    const double cb = (B.integrator == 1 ? 1000.0 : 1.0) * B.nwin * B.ioutInt;
+    return ca > cb;
+  });
+  std::vector<int64_t> order;
+  order.reserve((size_t)c->n);
+  for (int k : idx)
+    for (int64_t j = 0; j < c->sets_h[k].n; ++j) order.push_back(c->sets_h[k].first + j);
+  ST_CUDA(cudaMalloc(&c->order_d, sizeof(int64_t) * std::max<size_t>(order.size(), 1)));
+  ST_CUDA(cudaMemcpyAsync(c->order_d, order.data(), sizeof(int64_t) * order.size(), cudaMemcpyHostToDevice,
+                          c->stream));
+  return ST_OK;
+}
+
+st::RunArgs make_args(st_ctx* c, int w_begin, int w_end, void* snap) {
+  st::RunArgs a{};
+  a.sets = c->sets_d;
+  a.nsets = (int)c->sets_h.size();
+  a.order = c->order_d;
+  a.s = c->s;
+  a.status = c->status_d;
+  a.snap = (char*)snap;
+  a.snap_layout = c->snap;
+  a.w_begin = w_begin;
+  a.w_end = w_end;
+  a.deadline_armed = 0;
+  a.count_work = 1;
+  return a;
+}
+
+int begin_run(st_ctx* c) {
+  ST_CUDA(cudaSetDevice(c->device));
+  ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
+  return ST_OK;
+}
+
+// Arm the device time budget: a one-thread kernel stores %globaltimer + budget.
+int arm_deadline(st_ctx* c, st::RunArgs& a);
+
+int end_run(st_ctx* c, int launches) {
+  ST_CUDA(cudaMemcpyAsync(c->status_h, c->status_d, sizeof(st::RunStatus), cudaMemcpyDeviceToHost, c->stream));
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(ST_ERR_CUDA, std::string("kernel execution: ") + cudaGetErrorString(e));
+  c->last.dop_attempts = c->status_h->dop_attempts;
+  c->last.rk45_attempts = c->status_h->rk45_attempts;
+  c->last.segments = c->status_h->segments;
+  c->last.kernel_launches = (uint64_t)launches;
+  if (c->status_h->deadline_hit) return fail(ST_ERR_DEADLINE, "device time budget ran out; state saved at window ends");
+  return ST_OK;
+}
+
+}  // namespace
+
+namespace {
+int arm_deadline(st_ctx* c, st::RunArgs& a) {
+  if (c->deadline_s <= 0.0) return ST_OK;
+  int e = st::launch_arm_deadline(c->status_d, (unsigned long long)(c->deadline_s * 1e9), c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("arm deadline: ") + cudaGetErrorString((cudaError_t)e));
+  a.deadline_armed = 1;  // kernels read the armed value from the status block
+  return ST_OK;
+}
+
+// Autotuner: time each persistent-kernel variant and occupancy on a sample of
+// the context's own parameter sets (one window of a scratch context), keep the
+// fastest.
+int autotune(st_ctx* c);
+
+int run_persistent(st_ctx* c, int w_begin, int w_end, void* snap) {
+  ST_TRY(ctx_build_order(c));
+  if (c->lc.variant < 0 || c->lc.blocks_per_sm <= 0) ST_TRY(autotune(c));
+  st::RunArgs a = make_args(c, w_begin, w_end, snap);
+  ST_TRY(arm_deadline(c, a));
+  const int blocks = c->sm_count * c->lc.blocks_per_sm;
+  int e = st::launch_persistent(a, c->lc.variant, blocks, c->lc.block_threads, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString((cudaError_t)e));
+  return ST_OK;
+}
+
+int plain_block(const st_ctx* c) {
+  int b = c->opts.empty() ? 128 : c->opts[0].numPerGPUBlock;
+  return b > 0 ? b : 128;
+}
+
+}  // namespace
+
+// ==================================================================== C ABI
+extern "C" {
+
+int st_version(void) { return 1; }
+const char* st_last_error(void) { return g_err.c_str(); }
+size_t st_options_size(void) { return sizeof(st_options); }
+
+void st_options_default(st_options* o) {
+  std::memset(o, 0, sizeof(*o));  // padding bytes of the header image are zero
+  o->B0 = {3e-6, 0.0, 0.0};
+  o->E = {75e5, 0.0, 0.0};
+  o->L = {0.07, 0.1, 0.4};
+  o->yi = {0.0, 0.0, 1.0};
+  o->m = 1.20239e-26;
+  o->t0 = 0.0;
+  o->tf = 10.0;
+  o->rtol = 1e-12;
+  o->atol = 1e-12;
+  o->beta = 0.0;
+  o->uround = 1e-16;
+  o->safe = 0.9;
+  o->fac1 = 0.333;
+  o->fac2 = 6.0;
+  o->hmax = 1.0;
+  o->hmin = 1.0e-8;
+  o->h = 0.001;
+  o->T = 4.2;
+  o->gamma = -2.038e8;
+  o->V = 5.0;
+  o->swapStepSize = 1.0 - 4;  // the reference's default expression, -3
+  o->maxPosStep = 0.1;
+  o->ioutInt = 0.05;
+  o->diffuse = 1.0;
+  o->nmax = 10000000u;
+  o->seed = 0u;
+  o->integratorType = 0;
+  o->numParticles = 1000;
+  o->numPerGPUBlock = 128;
+  o->iout = 2;
+  o->dist = 'C';
+  o->gas_coll = true;
+  o->gravity = true;
+  o->fixedStepSize = false;
+  o->keepStepSize = false;
+}
+
+int st_parse_line(st_options* o, const char* line) {
+  if (!o || !line) return fail(ST_ERR_ARG, "null argument");
+  std::vector<std::string> e = split_fields(line);
+  if (e.size() < 2) return fail(ST_ERR_ARG, std::string("Misunderstood input line in options file: ") + line);
+  const std::string& k = e[0];
+  auto num = [&](size_t i, double* v) -> bool {
+    if (i >= e.size() || !to_double(e[i], v)) {
+      fail(ST_ERR_ARG, "malformed number in line: " + std::string(line));
+      return false;
+    }
+    return true;
+  };
+  auto vec = [&](st_vec3* v) -> int {
+    double a, b, cc;
+    if (!num(1, &a) || !num(2, &b) || !num(3, &cc)) return ST_ERR_ARG;
+    *v = {a, b, cc};
+    return ST_OK;
+  };
+  auto dbl = [&](double* v) -> int { return num(1, v) ? ST_OK : ST_ERR_ARG; };
+  auto integer = [&](int* v) -> int {
+    if (!to_int(e[1], v)) return fail(ST_ERR_ARG, "malformed integer in line: " + std::string(line));
+    return ST_OK;
+  };
+  auto uinteger = [&](unsigned int* v) -> int {
+    int x;
+    if (!to_int(e[1], &x)) return fail(ST_ERR_ARG, "malformed integer in line: " + std::string(line));
+    *v = (unsigned int)x;
+    return ST_OK;
+  };
+  // keys of src/optionsParser.cpp:50-170
+  if (k == "L") return vec(&o->L);
+  if (k == "yi") return vec(&o->yi);
+  if (k == "Gx") return vec(&o->Gx);
+  if (k == "Gy") return vec(&o->Gy);
+  if (k == "Gz") return vec(&o->Gz);
+  if (k == "dist") {
+    o->dist = e[1].empty() ? '\0' : e[1][0];
+    return ST_OK;
+  }
+  if (k == "m") return dbl(&o->m);
+  if (k == "gas_coll") { o->gas_coll = to_bool(e[1]); return ST_OK; }
+  if (k == "T") return dbl(&o->T);
+  if (k == "diffuse") return dbl(&o->diffuse);
+  if (k == "gamma") return dbl(&o->gamma);
+  if (k == "V") return dbl(&o->V);
+  if (k == "a") return dbl(&o->a);
+  if (k == "w") return dbl(&o->w);
+  if (k == "gravity") { o->gravity = to_bool(e[1]); return ST_OK; }
+  if (k == "fixedStepSize") { o->fixedStepSize = to_bool(e[1]); return ST_OK; }
+  if (k == "keepStepSize") { o->keepStepSize = to_bool(e[1]); return ST_OK; }
+  if (k == "B0") return vec(&o->B0);
+  if (k == "E") return vec(&o->E);
+  if (k == "t0") return dbl(&o->t0);
+  if (k == "tf") return dbl(&o->tf);
+  if (k == "rtol") return dbl(&o->rtol);
+  if (k == "atol") return dbl(&o->atol);
+  if (k == "beta") return dbl(&o->beta);
+  if (k == "uround") return dbl(&o->uround);
+  if (k == "safe") return dbl(&o->safe);
+  if (k == "fac1") return dbl(&o->fac1);
+  if (k == "fac2") return dbl(&o->fac2);
+  if (k == "hmax") return dbl(&o->hmax);
+  if (k == "hmin") return dbl(&o->hmin);
+  if (k == "h") return dbl(&o->h);
+  if (k == "nmax") return uinteger(&o->nmax);
+  if (k == "seed") return uinteger(&o->seed);
+  if (k == "maxPosStep") return dbl(&o->maxPosStep);
+  if (k == "integratorType") return integer(&o->integratorType);
+  if (k == "swapStepSize") return dbl(&o->swapStepSize);
+  if (k == "numParticles") return integer(&o->numParticles);
+  if (k == "numPerGPUBlock") return integer(&o->numPerGPUBlock);
+  if (k == "ioutInt") return dbl(&o->ioutInt);
+  if (k == "iout") return integer(&o->iout);
+  g_err = "Unrecognized Option: " + k + " (line ignored)";
+  return 1;
+}
+
+int st_parse_params(const char* path, st_options* o) {
+  if (!o || !path) return fail(ST_ERR_ARG, "null argument");
+  st_options_default(o);
+  FILE* f = std::fopen(path, "r");
+  if (!f) return fail(ST_ERR_IO, std::string("cannot open params file ") + path + " (defaults kept)");
+  std::string line;
+  int c;
+  int lineno = 0;
+  int rc = ST_OK;
+  auto flush = [&]() {
+    ++lineno;
+    int r = st_parse_line(o, line.c_str());
+    if (r == 1) {
+      std::fprintf(stderr, "Unrecognized Option: %s\nLine Ignored\n", split_fields(line.c_str())[0].c_str());
+    } else if (r != ST_OK) {
+      const std::vector<std::string> e = split_fields(line.c_str());
+      if (e.size() >= 2 && rc == ST_OK) {
+        rc = fail(ST_ERR_ARG, std::string(path) + ":" + std::to_string(lineno) + ": " + g_err);
+      }
+      // lines with fewer than two fields are skipped, as the reference does
+    }
+    line.clear();
+  };
+  while ((c = std::fgetc(f)) != EOF) {
+    if (c == '\n')
+      flush();
+    else
+      line.push_back((char)c);
+  }
+  if (!line.empty()) flush();
+  std::fclose(f);
+  return rc;
+}
+
+void st_derive(st_options* o) {
+  const double k = 1.380649e-23;  // src/simulation.cpp:9-11
+  o->tc = 1.6e-4 * o->m / (k * std::pow(o->T, 8.0));
+  o->sqrtKT_m = std::sqrt(k * o->T / o->m);
+}
+
+int st_num_windows(const st_options* o) {
+  const double q = std::floor((double)(o->tf - o->t0) / o->ioutInt);
+  if (!(q > 0.0)) return 0;
+  if (q > 2147483647.0) return 2147483647;
+  return (int)q;
+}
+
+int st_create_batch(const st_options* sets, int nsets, int device, st_ctx** out) {
+  if (!out || (!sets && nsets > 0) || nsets < 1) return fail(ST_ERR_ARG, "need at least one parameter set");
+  *out = nullptr;
+  st_ctx* c = new st_ctx();
+  c->device = device;
+  int64_t first = 0;
+  for (int k = 0; k < nsets; ++k) {
+    SetParams P;
+    int r = build_params(sets[k], first, &P);
+    if (r != ST_OK) {
+      delete c;
+      return r;
+    }
+    c->opts.push_back(sets[k]);
+    c->sets_h.push_back(P);
+    first += sets[k].numParticles;
+  }
+  c->n = first;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(ST_ERR_CUDA, std::string("device setup: ") + cudaGetErrorString(e));
+  }
+  int r = ctx_alloc(c);
+  if (r != ST_OK) {
+    st_destroy(c);
+    return r;
+  }
+  *out = c;
+  return ST_OK;
+}
+
+int st_create(const st_options* opt, int device, st_ctx** out) {
+  if (!opt) return fail(ST_ERR_ARG, "null options");
+  return st_create_batch(opt, 1, device, out);
+}
+
+void st_destroy(st_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->arena);
+  cudaFree(c->sets_d);
+  cudaFree(c->status_d);
+  cudaFree(c->order_d);
+  if (c->status_h) cudaFreeHost(c->status_h);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int st_init(st_ctx* c) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  ST_CUDA(cudaSetDevice(c->device));
+  st::RunArgs a = make_args(c, 0, 0, nullptr);
+  int e = st::launch_init(a, 256, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("init launch: ") + cudaGetErrorString((cudaError_t)e));
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  c->initialized = true;
+  c->window_grid = true;
+  return ST_OK;
+}
+
+int st_run_until(st_ctx* c, double next_t) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  if (!c->initialized) return fail(ST_ERR_STATE, "st_run_until before st_init");
+  ST_TRY(begin_run(c));
+  st::RunArgs a = make_args(c, 0, 0, nullptr);
+  ST_TRY(arm_deadline(c, a));
+  int e = st::launch_until(a, next_t, plain_block(c), c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("plain launch: ") + cudaGetErrorString((cudaError_t)e));
+  c->window_grid = false;
+  return end_run(c, 1);
+}
+
+int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  if (!c->initialized) return fail(ST_ERR_STATE, "st_run_windows before st_init");
+  if (!c->window_grid) return fail(ST_ERR_STATE, "particles were advanced off the window grid by st_run_until");
+  if (w_begin < 0 || w_end < w_begin) return fail(ST_ERR_ARG, "bad window range");
+  if (w_end == w_begin) return ST_OK;
+  ST_TRY(begin_run(c));
+  int launches = 0;
+  if (kernel == ST_KERNEL_PLAIN) {
+    st::RunArgs a = make_args(c, w_begin, w_end, snap);
+    ST_TRY(arm_deadline(c, a));
+    for (int w = w_begin; w < w_end; ++w) {
+      int e = st::launch_plain_window(a, w, plain_block(c), c->stream);
+      if (e) return fail(ST_ERR_CUDA, std::string("plain launch: ") + cudaGetErrorString((cudaError_t)e));
+      ++launches;
+      if (snap) {
+        e = st::launch_pack_snapshot(a, w - w_begin, c->stream);
+        if (e) return fail(ST_ERR_CUDA, std::string("pack launch: ") + cudaGetErrorString((cudaError_t)e));
+        ++launches;
+      }
+    }
+  } else if (kernel == ST_KERNEL_PERSISTENT) {
+    ST_TRY(run_persistent(c, w_begin, w_end, snap));
+    ++launches;
+  } else {
+    return fail(ST_ERR_ARG, "unknown kernel selector");
+  }
+  return end_run(c, launches);
+}
+
+size_t st_snapshot_bytes(const st_ctx* c) { return c ? c->snap.bytes : 0; }
+size_t st_snapshot_field_offset(const st_ctx* c, int f) { return (c && f >= 0 && f < 14) ? c->snap.off[f] : 0; }
+
+int st_read_state(st_ctx* c, const st_state_view* h) {
+  if (!c || !h) return fail(ST_ERR_ARG, "null argument");
+  ST_CUDA(cudaSetDevice(c->device));
+  const size_t n = (size_t)c->n;
+  if (n == 0) return ST_OK;
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<double> tmp(n);
+  auto get = [&](const void* src, void* dst, size_t bytes) -> int {
+    ST_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return ST_OK;
+  };
+  auto get3 = [&](double* const xs, double* const ys, double* const zs, st_vec3* dst) -> int {
+    if (!dst) return ST_OK;
+    ST_TRY(get(xs, tmp.data(), 8 * n));
+    for (size_t i = 0; i < n; ++i) dst[i].x = tmp[i];
+    ST_TRY(get(ys, tmp.data(), 8 * n));
+    for (size_t i = 0; i < n; ++i) dst[i].y = tmp[i];
+    ST_TRY(get(zs, tmp.data(), 8 * n));
+    for (size_t i = 0; i < n; ++i) dst[i].z = tmp[i];
+    return ST_OK;
+  };
+  if (h->t) ST_TRY(get(c->s.t, h->t, 8 * n));
+  ST_TRY(get3(c->s.px, c->s.py, c->s.pz, h->pos));
+  ST_TRY(get3(c->s.vx, c->s.vy, c->s.vz, h->v));
+  ST_TRY(get3(c->s.Sx, c->s.Sy, c->s.Sz, h->S));
+  if (h->fail) ST_TRY(get(c->s.fail, h->fail, 4 * n));
+  if (h->n_coll) ST_TRY(get(c->s.n_coll, h->n_coll, 8 * n));
+  if (h->n_bounce) ST_TRY(get(c->s.n_bounce, h->n_bounce, 8 * n));
+  if (h->n_steps) ST_TRY(get(c->s.n_steps, h->n_steps, 8 * n));
+  return ST_OK;
+}
+
+int st_device_state(st_ctx* c, st_device_soa* o) {
+  if (!c || !o) return fail(ST_ERR_ARG, "null argument");
+  o->n_total = c->n;
+  o->t = c->s.t;
+  o->pos_x = c->s.px; o->pos_y = c->s.py; o->pos_z = c->s.pz;
+  o->v_x = c->s.vx; o->v_y = c->s.vy; o->v_z = c->s.vz;
+  o->S_x = c->s.Sx; o->S_y = c->s.Sy; o->S_z = c->s.Sz;
+  o->h = c->s.h;
+  o->next_gas = c->s.next_gas;
+  o->fail = c->s.fail;
+  o->n_coll = c->s.n_coll; o->n_bounce = c->s.n_bounce; o->n_steps = c->s.n_steps;
+  o->stop = c->s.stop;
+  return ST_OK;
+}
+
+int st_synchronize(st_ctx* c) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  return ST_OK;
+}
+
+int st_set_launch_config(st_ctx* c, const st_launch_config* cfg) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  if (!cfg) {
+    c->lc = {0, 0, -1};
+    return ST_OK;
+  }
+  if (cfg->variant >= st::persistent_variant_count()) return fail(ST_ERR_ARG, "no such kernel variant");
+  c->lc = *cfg;
+  if (c->lc.variant >= 0 && c->lc.blocks_per_sm <= 0) {
+    c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, 0));
+  }
+  return ST_OK;
+}
+
+int st_get_launch_config(const st_ctx* c, st_launch_config* cfg) {
+  if (!c || !cfg) return fail(ST_ERR_ARG, "null argument");
+  *cfg = c->lc;
+  return ST_OK;
+}
+
+int st_set_deadline(st_ctx* c, double seconds) {
+  if (!c || !(seconds >= 0.0)) return fail(ST_ERR_ARG, "bad deadline");
+  c->deadline_s = seconds;
+  return ST_OK;
+}
+
+int st_get_counters(const st_ctx* c, st_counters* out) {
+  if (!c || !out) return fail(ST_ERR_ARG, "null argument");
+  *out = c->last;
+  return ST_OK;
+}
+
+int st_probe_fp64_peak(int device, double* tflops) {
+  if (!tflops) return fail(ST_ERR_ARG, "null argument");
+  ST_CUDA(cudaSetDevice(device));
+  int sms = 0;
+  ST_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  double best = 0.0;
+  for (int rep = 0; rep < 3; ++rep) {
+    double sec = 0.0, flops = 0.0;
+    int e = st::probe_fp64(sms, 1 << 14, &sec, &flops);
+    if (e) return fail(ST_ERR_CUDA, std::string("fp64 probe: ") + cudaGetErrorString((cudaError_t)e));
+    if (sec > 0.0) best = std::max(best, flops / sec * 1e-12);
+  }
+  *tflops = best;
+  return ST_OK;
+}
+
+int st_write_header(void* file, const st_options* opt) {
+  FILE* f = (FILE*)file;
+  if (!f || !opt) return fail(ST_ERR_ARG, "null argument");
+  st_options img = *opt;
+  // zero the three padding bytes after keepStepSize so files are reproducible
+  unsigned char* b = reinterpret_cast<unsigned char*>(&img);
+  const size_t pad0 = offsetof(st_options, keepStepSize) + 1;
+  std::memset(b + pad0, 0, offsetof(st_options, noiseAmplitudes) - pad0);
+  if (std::fwrite(&img, sizeof(img), 1, f) != 1) return fail(ST_ERR_IO, "header write failed");
+  return ST_OK;
+}
+
+int st_write_snapshot(void* file, int n, const st_state_view* h) {
+  FILE* f = (FILE*)file;
+  if (!f || !h || n < 0) return fail(ST_ERR_ARG, "bad argument");
+  const size_t m = (size_t)n;
+  bool ok = true;
+  ok = ok && std::fwrite(h->t, 8, m, f) == m;
+  ok = ok && std::fwrite(h->pos, 24, m, f) == m;
+  ok = ok && std::fwrite(h->v, 24, m, f) == m;
+  ok = ok && std::fwrite(h->S, 24, m, f) == m;
+  ok = ok && std::fwrite(h->fail, 4, m, f) == m;
+  ok = ok && std::fwrite(h->n_coll, 8, m, f) == m;
+  ok = ok && std::fwrite(h->n_bounce, 8, m, f) == m;
+  ok = ok && std::fwrite(h->n_steps, 8, m, f) == m;
+  return ok ? ST_OK : fail(ST_ERR_IO, "snapshot write failed");
+}
+
+}  // extern "C"
+
+// ==================================================================== driver
+namespace {
+
+struct HostSnap {
+  std::vector<double> t;
+  std::vector<st_vec3> pos, v, S;
+  std::vector<int32_t> fail;
+  std::vector<uint64_t> n_coll, n_bounce, n_steps;
+  explicit HostSnap(size_t n) : t(n), pos(n), v(n), S(n), fail(n), n_coll(n), n_bounce(n), n_steps(n) {}
+  st_state_view view() {
+    return st_state_view{t.data(), pos.data(), v.data(), S.data(), fail.data(), n_coll.data(), n_bounce.data(),
+                         n_steps.data()};
+  }
+};
+
+// Unpack one device snapshot block (already copied to host memory).
+void unpack_block(const st_ctx* c, const char* blk, HostSnap& hs) {
+  const size_t n = (size_t)c->n;
+  const double* f[10];
+  for (int k = 0; k < 10; ++k) f[k] = reinterpret_cast<const double*>(blk + c->snap.off[k]);
+  std::memcpy(hs.t.data(), f[0], 8 * n);
+  for (size_t i = 0; i < n; ++i) {
+    hs.pos[i] = {f[1][i], f[2][i], f[3][i]};
+    hs.v[i] = {f[4][i], f[5][i], f[6][i]};
+    hs.S[i] = {f[7][i], f[8][i], f[9][i]};
+  }
+  std::memcpy(hs.fail.data(), blk + c->snap.off[10], 4 * n);
+  std::memcpy(hs.n_coll.data(), blk + c->snap.off[11], 8 * n);
+  std::memcpy(hs.n_bounce.data(), blk + c->snap.off[12], 8 * n);
+  std::memcpy(hs.n_steps.data(), blk + c->snap.off[13], 8 * n);
+}
+
+}  // namespace
+
+extern "C" int st_main_analysis(const st_options* opt_in, const char* out_path, int device, int kernel,
+                                double* run_seconds) {
+  if (!opt_in || !out_path) return fail(ST_ERR_ARG, "null argument");
+  st_options opt = *opt_in;
+  st_derive(&opt);
+  st_ctx* c = nullptr;
+  ST_TRY(st_create(&opt, device, &c));
+  struct Guard {
+    st_ctx* c;
+    FILE* f;
+    void* snap_d;
+    void* snap_h;
+    ~Guard() {
+      if (f) std::fclose(f);
+      if (snap_d) cudaFree(snap_d);
+      if (snap_h) cudaFreeHost(snap_h);
+      st_destroy(c);
+    }
+  } g{c, nullptr, nullptr, nullptr};
+  ST_TRY(st_init(c));
+  g.f = std::fopen(out_path, "wb");
+  if (!g.f) return fail(ST_ERR_IO, std::string("cannot open ") + out_path);
+  ST_TRY(st_write_header(g.f, &opt));
+  const size_t n = (size_t)c->n;
+  HostSnap hs(n);
+  st_state_view hv = hs.view();
+  ST_TRY(st_read_state(c, &hv));
+  ST_TRY(st_write_snapshot(g.f, (int)n, &hv));
+  const int nwin = st_num_windows(&opt);
+  double run = 0.0;
+  if (kernel == ST_KERNEL_PLAIN) {
+    for (int w = 0; w < nwin; ++w) {
+      const double t0 = now_s();
+      ST_TRY(st_run_windows(c, ST_KERNEL_PLAIN, w, w + 1, nullptr));
+      run += now_s() - t0;
+      ST_TRY(st_read_state(c, &hv));
+      ST_TRY(st_write_snapshot(g.f, (int)n, &hv));
+    }
+  } else {
+    // windows in chunks whose snapshot blocks fit a quarter of free memory
+    size_t free_b = 0, total_b = 0;
+    ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t blk = st_snapshot_bytes(c);
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nwin, 1), (free_b / 4) / std::max<size_t>(blk, 1)));
+    ST_CUDA(cudaMalloc(&g.snap_d, blk * (size_t)chunk));
+    ST_CUDA(cudaMallocHost(&g.snap_h, blk * (size_t)chunk));
+    for (int w = 0; w < nwin; w += chunk) {
+      const int we = std::min(nwin, w + chunk);
+      const double t0 = now_s();
+      ST_TRY(st_run_windows(c, kernel, w, we, g.snap_d));
+      run += now_s() - t0;
+      ST_CUDA(cudaMemcpy(g.snap_h, g.snap_d, blk * (size_t)(we - w), cudaMemcpyDeviceToHost));
+      for (int k = 0; k < we - w; ++k) {
+        unpack_block(c, (const char*)g.snap_h + blk * (size_t)k, hs);
+        ST_TRY(st_write_snapshot(g.f, (int)n, &hv));
+      }
+    }
+  }
+  if (run_seconds) *run_seconds = run;
+  return ST_OK;
+}
+
+// ==================================================================== autotune
+namespace {
+
+int autotune(st_ctx* c) {
+  const int nv = st::persistent_variant_count();
+  // sample: a few particles of every set, one window, on a scratch context
+  std::vector<st_options> sample = c->opts;
+  const int64_t lanes_guess = (int64_t)c->sm_count * 256;
+  const int64_t want = std::max<int64_t>(4 * lanes_guess, 1);
+  const double frac = std::min(1.0, (double)want / (double)std::max<int64_t>(c->n, 1));
+  for (auto& o : sample) {
+    o.numParticles = std::max(0, (int)std::ceil(o.numParticles * frac));
+    o.tf = o.t0 + o.ioutInt;  // one window
+  }
+  st_ctx* s = nullptr;
+  ST_TRY(st_create_batch(sample.data(), (int)sample.size(), c->device, &s));
+  double best = 1e300;
+  st_launch_config best_cfg{0, 1, 0};
+  for (int v = 0; v < nv; ++v) {
+    const int maxb = st::persistent_max_blocks_per_sm(v, 0);
+    for (int b = 1; b <= std::max(1, maxb); ++b) {
+      st_launch_config cfg{0, b, v};
+      st_set_launch_config(s, &cfg);
+      if (st_init(s) != ST_OK) break;
+      const double t0 = now_s();
+      const int r = st_run_windows(s, ST_KERNEL_PERSISTENT, 0, 1, nullptr);
+      const double el = now_s() - t0;
+      if (r != ST_OK) continue;
+      if (el < best) {
+        best = el;
+        best_cfg = cfg;
+      }
+    }
+  }
+  st_destroy(s);
+  c->lc = best_cfg;
+  return ST_OK;
+}
+
+}  // namespace

@@ -1,0 +1,733 @@
+// Device building blocks of the hot path: the RNG, the ballistic trajectory
+// events, the field polynomial and single step attempts of DOP853 and RK45.
+//
+// Two arithmetic regimes:
+//  * Trajectory and RNG code reproduces the reference's doubles bit for bit
+//    (same operation order, no FMA contraction: every add/mul/div/sqrt is an
+//    explicit round-to-nearest intrinsic), so event times, bounce/collision
+//    counts and RNG draws match the CPU build exactly.  Only CUDA's log / acos /
+//    cos / sin may differ from libm by an ulp.
+//  * The spin steppers are restated for the FP64 pipe: FMA-contracted stage
+//    sums, the field as a polynomial in segment time, reciprocal-form error
+//    weights and step controller.  Results agree with the reference to the
+//    integration tolerance, not bit for bit.
+#pragma once
+
+#include <float.h>
+#include <stdint.h>
+#include "st_internal.h"
+#include "st_fields.cuh"
+#include "st_tableau.h"
+
+namespace st {
+
+// ------------------------------------------------------------------ exact ops
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
+// sgn with sgn(0) = +1 (src/particle.cpp:24-31)
+__device__ __forceinline__ double sgn1(double v) { return v < 0.0 ? -1.0 : 1.0; }
+// std::min / std::max argument conventions
+__device__ __forceinline__ double std_min(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double std_max(double a, double b) { return (a < b) ? b : a; }
+// min_d / max_d (src/integrator.cpp:25-33)
+__device__ __forceinline__ double min_d(double a, double b) { return (a < b) ? a : b; }
+__device__ __forceinline__ double max_d(double a, double b) { return (a > b) ? a : b; }
+
+// ------------------------------------------------------------ fast FP64 roots
+// Approximate hardware seeds (PTX rcp.approx / rsqrt.approx, ~2^-22 relative)
+// refined by FMA Newton steps on the FP64 pipe.
+__device__ __forceinline__ double rcp_seed(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+}
+__device__ __forceinline__ double rsqrt_seed(double x) {
+  double r;
+  asm("rsqrt.approx.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+}
+// 1/x to full double precision for finite nonzero x; 0 and inf pass through.
+__device__ __forceinline__ double rcp_full(double x) {
+  const double r = rcp_seed(x);
+  const double e = fma(-x, r, 1.0);
+  const double r2 = fma(r, fma(e, e, e), r);  // third-order correction
+  return (e == e) ? r2 : r;
+}
+// 1/sqrt(x) to full double precision for finite positive x.
+__device__ __forceinline__ double rsqrt_full(double x) {
+  const double y = rsqrt_seed(x);
+  const double e = fma(-x * y, y, 1.0);
+  const double y2 = fma(y * e, fma(0.375, e, 0.5), y);  // third-order correction
+  return (e == e) ? y2 : y;
+}
+// x^(-1/8) for 1e-300 < x < 1e300: chained rsqrt seeds, two Newton steps on
+// r^8 x = 1.
+__device__ __forceinline__ double rroot8(double x) {
+  double r = rsqrt_seed(rsqrt_seed(rsqrt_seed(x)));
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double r2 = r * r, r4 = r2 * r2;
+    const double u = (r4 * r4) * x;
+    r = fma(r, fma(u, -0.125, 0.125), r);
+  }
+  return r;
+}
+
+// ------------------------------------------------------------------------ RNG
+// Reference rngState (include/particle.h:52-59) and its generator.
+struct Rng {
+  uint64_t x, y, z, w;
+  double spare;
+  bool has;
+};
+
+// xoshiro256+ as the reference implements it (src/particle.cpp:59-70): the
+// last word is re-derived from the third, not rotated in place.
+__device__ __forceinline__ uint64_t rng_next(Rng& r) {
+  const uint64_t out = r.x + r.z;
+  const uint64_t t = r.y << 17;
+  r.z ^= r.x;
+  r.w ^= r.y;
+  r.y ^= r.z;
+  r.x ^= r.w;
+  r.z ^= t;
+  r.w = (r.z << 45) | (r.z >> 19);
+  return out;
+}
+// top 53 bits scaled by 2^-53 (exact), src/particle.cpp:72-83
+__device__ __forceinline__ double rng_uniform(Rng& r) { return xmul((double)(rng_next(r) >> 11), 0x1.0p-53); }
+
+// Marsaglia polar normal with cached spare (src/particle.cpp:89-107).
+__device__ __forceinline__ double rng_normal(Rng& r, double mean, double sd) {
+  if (r.has) {
+    r.has = false;
+    return xadd(xmul(r.spare, sd), mean);
+  }
+  double u, v, s;
+  do {
+    u = xadd(xmul(rng_uniform(r), 2.0), -1.0);
+    v = xadd(xmul(rng_uniform(r), 2.0), -1.0);
+    s = xadd(xmul(u, u), xmul(v, v));
+  } while (s >= 1.0 || s == 0.0);
+  s = xsqrt(xdiv(xmul(-2.0, log(s)), s));
+  r.spare = xmul(v, s);
+  r.has = true;
+  return xadd(mean, xmul(xmul(sd, u), s));
+}
+__device__ __forceinline__ double rng_exponential(Rng& r, double tc) {
+  return xmul(-tc, log(xsub(1.0, rng_uniform(r))));
+}
+
+// Seeding of initParticlesCPU (src/particle.cpp:648-663): splitmix64 of the
+// 32-bit sum seed + ipart, two outputs split into 32-bit halves, three
+// discarded draws.
+__device__ __forceinline__ uint64_t splitmix_next(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ Rng rng_seed(unsigned int seed, unsigned int ipart) {
+  uint64_t s = (uint64_t)(uint32_t)(seed + ipart);
+  Rng r;
+  const uint64_t a = splitmix_next(s);
+  r.x = (uint32_t)a;
+  r.y = (uint32_t)(a >> 32);
+  const uint64_t b = splitmix_next(s);
+  r.z = (uint32_t)b;
+  r.w = (uint32_t)(b >> 32);
+  r.spare = 0.0;
+  r.has = false;
+  rng_next(r);
+  rng_next(r);
+  rng_next(r);
+  return r;
+}
+
+// ------------------------------------------------------------ particle state
+struct PState {
+  double t, px, py, pz, vx, vy, vz, Sx, Sy, Sz, h, next_gas;
+  Rng rng;
+  uint64_t n_coll, n_bounce, n_steps;
+  int fail;
+  bool stop;
+  char coll, wall;
+};
+
+__device__ __forceinline__ PState load_state(const DeviceState& s, int64_t i) {
+  PState p;
+  p.t = s.t[i];
+  p.px = s.px[i]; p.py = s.py[i]; p.pz = s.pz[i];
+  p.vx = s.vx[i]; p.vy = s.vy[i]; p.vz = s.vz[i];
+  p.Sx = s.Sx[i]; p.Sy = s.Sy[i]; p.Sz = s.Sz[i];
+  p.h = s.h[i];
+  p.next_gas = s.next_gas[i];
+  p.rng.x = s.rx[i]; p.rng.y = s.ry[i]; p.rng.z = s.rz[i]; p.rng.w = s.rw[i];
+  p.rng.spare = s.rspare[i];
+  p.rng.has = s.rhas[i] != 0;
+  p.n_coll = s.n_coll[i]; p.n_bounce = s.n_bounce[i]; p.n_steps = s.n_steps[i];
+  p.fail = s.fail[i];
+  p.stop = s.stop[i] != 0;
+  p.coll = (char)s.coll[i];
+  p.wall = (char)s.wall[i];
+  return p;
+}
+
+__device__ __forceinline__ void store_state(const DeviceState& s, int64_t i, const PState& p) {
+  s.t[i] = p.t;
+  s.px[i] = p.px; s.py[i] = p.py; s.pz[i] = p.pz;
+  s.vx[i] = p.vx; s.vy[i] = p.vy; s.vz[i] = p.vz;
+  s.Sx[i] = p.Sx; s.Sy[i] = p.Sy; s.Sz[i] = p.Sz;
+  s.h[i] = p.h;
+  s.next_gas[i] = p.next_gas;
+  s.rx[i] = p.rng.x; s.ry[i] = p.rng.y; s.rz[i] = p.rng.z; s.rw[i] = p.rng.w;
+  s.rspare[i] = p.rng.spare;
+  s.rhas[i] = p.rng.has ? 1 : 0;
+  s.n_coll[i] = p.n_coll; s.n_bounce[i] = p.n_bounce; s.n_steps[i] = p.n_steps;
+  s.fail[i] = p.fail;
+  s.stop[i] = p.stop ? 1 : 0;
+  s.coll[i] = (uint8_t)p.coll;
+  s.wall[i] = (uint8_t)p.wall;
+}
+
+// initParticlesCPU for one particle (src/particle.cpp:646-708).
+__device__ inline PState init_particle(const SetParams& P, unsigned int ipart) {
+  PState p;
+  Rng r = rng_seed(P.seed, ipart);
+  p.px = xsub(xmul(rng_uniform(r), P.Lx), P.Lx / 2.0);
+  p.py = xsub(xmul(rng_uniform(r), P.Ly), P.Ly / 2.0);
+  p.pz = xsub(xmul(rng_uniform(r), P.Lz), P.Lz / 2.0);
+  p.next_gas = P.gas ? rng_exponential(r, P.tc) : DBL_MAX;
+  p.vx = p.vy = p.vz = 0.0;
+  if (P.dist == 'C') {
+    // the CPU build draws three normals even for V == 0 (src/particle.cpp:677-684)
+    const double dx = rng_normal(r, 0.0, 1.0);
+    const double dy = rng_normal(r, 0.0, 1.0);
+    const double dz = rng_normal(r, 0.0, 1.0);
+    const double nrm = xsqrt(xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz)));
+    p.vx = xdiv(xmul(dx, P.V), nrm);
+    p.vy = xdiv(xmul(dy, P.V), nrm);
+    p.vz = xdiv(xmul(dz, P.V), nrm);
+  } else if (P.dist == 'M') {
+    p.vx = xmul(rng_normal(r, 0.0, 1.0), P.sqrtKT_m);
+    p.vy = xmul(rng_normal(r, 0.0, 1.0), P.sqrtKT_m);
+    p.vz = xmul(rng_normal(r, 0.0, 1.0), P.sqrtKT_m);
+  }
+  p.rng = r;
+  p.Sx = P.yi_x; p.Sy = P.yi_y; p.Sz = P.yi_z;
+  p.t = P.t0;
+  p.h = P.h0;
+  p.stop = false;
+  p.coll = 'W';
+  p.wall = 0;
+  p.fail = 0;
+  p.n_coll = p.n_bounce = p.n_steps = 0;
+  return p;
+}
+
+// Start of the current ballistic segment (t_old, pos_old, v_old).
+struct SegStart {
+  double t, px, py, pz, vx, vy, vz;
+};
+
+// One trajectory event: calc_next_collision_time, update_position_and_velocity
+// and sanity_check (src/particle.cpp:121-444).  Returns `finished` (the window
+// end tf was reached).  Fills the segment start.
+__device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double tf, SegStart& s0) {
+  const double G = kGravity;
+  const double hLx = P.Lx / 2.0, hLy = P.Ly / 2.0, hLz = P.Lz / 2.0;
+  double dtx, dty, dtz;
+  // ---- time to the next wall (calc_next_collision_time)
+  if (P.gravity) {
+    const double dx = xsub(sgn1(p.vx) < 0.0 ? -hLx : hLx, p.px);
+    const double dz = xsub(sgn1(p.vz) < 0.0 ? -hLz : hLz, p.pz);
+    dtx = xdiv(dx, p.vx);
+    dtz = xdiv(dz, p.vz);
+    const double y2 = xmul(p.vy, p.vy);
+    if (sgn1(p.vy) <= 0.0) {  // moving down: the floor
+      const double dy = xadd(p.py, xmul(P.Ly, 0.5));
+      const double sq = xsqrt(xadd(xmul(-2.0 * G, dy), y2));
+      const double r1 = xdiv(-xadd(sq, p.vy), G);
+      const double r2 = xdiv(xsub(sq, p.vy), G);
+      dty = std_min(fabs(r1), fabs(r2));
+    } else {
+      const double top = xadd(xdiv(xmul(-0.5, y2), G), p.py);
+      if (top < xmul(0.5, P.Ly)) {  // apex below the ceiling: rise, then fall to the floor
+        const double t1 = xdiv(-p.vy, G);
+        const double apex = xadd(xadd(p.py, xmul(p.vy, t1)), xmul(xmul(0.5 * G, t1), t1));
+        const double t2 = xsqrt(xdiv(xmul(xsub(xmul(-0.5, P.Ly), apex), 2.0), G));
+        dty = xadd(t1, t2);
+      } else {  // reaches the ceiling
+        const double sq = xsqrt(xsub(y2, xmul(2.0 * G, xsub(p.py, xmul(0.5, P.Ly)))));
+        const double r1 = xdiv(xadd(-p.vy, sq), G);
+        const double r2 = xdiv(xsub(-p.vy, sq), G);
+        dty = std_min(fabs(r1), fabs(r2));
+      }
+    }
+    if (dtx < 1e-16 || isnan(dtx))  // only the first offending axis is replaced
+      dtx = 1e6;
+    else if (dty < 1e-16 || isnan(dty))
+      dty = 1e6;
+    else if (dtz < 1e-16 || isnan(dtz))
+      dtz = 1e6;
+  } else {
+    dtx = xdiv(xsub(sgn1(p.vx) < 0.0 ? -hLx : hLx, p.px), p.vx);
+    dty = xdiv(xsub(sgn1(p.vy) < 0.0 ? -hLy : hLy, p.py), p.vy);
+    dtz = xdiv(xsub(sgn1(p.vz) < 0.0 ? -hLz : hLz, p.pz), p.vz);
+    if (dtx < 1e-16)
+      dtx = 1e6;
+    else if (dty < 1e-16)
+      dty = 1e6;
+    else if (dtz < 1e-16)
+      dtz = 1e6;
+  }
+  double tb = __longlong_as_double(0x7ff8000000000000ll);  // unset when every comparison fails (NaN input)
+  if (dtx < dty && dtx < dtz) {
+    tb = dtx; p.wall = 'x';
+  } else if (dty < dtx && dty < dtz) {
+    tb = dty; p.wall = 'y';
+  } else if (dtz < dtx && dtz < dty) {
+    tb = dtz; p.wall = 'z';
+  } else if (dtx == dty && dtx == dtz) {
+    tb = dtx; p.wall = 'a';  // corner
+  } else if (dtx == dty) {
+    tb = dtx; p.wall = 'b';  // x-y edge
+  } else if (dtx == dtz) {
+    tb = dtx; p.wall = 'c';  // x-z edge
+  } else if (dty == dtz) {
+    tb = dty; p.wall = 'd';  // y-z edge
+  }
+  // ---- gas collision, wall, window end or maxPosStep
+  const double to_gas = xsub(p.next_gas, p.t);
+  bool gas_next;
+  double to_col;
+  if (to_gas < tb) {
+    gas_next = true;
+    to_col = to_gas;
+  } else if (to_gas == tb) {  // tie: the wall wins and the gas clock is redrawn
+    p.next_gas = xadd(p.next_gas, rng_exponential(p.rng, P.tc));
+    to_col = to_gas;
+    gas_next = false;
+  } else {
+    gas_next = false;
+    to_col = tb;
+  }
+  const double left = xsub(tf, p.t);
+  const bool window_end = left <= P.maxPosStep;
+  const double to_free = window_end ? left : P.maxPosStep;
+  bool finished = false;
+  double dt;
+  if (to_col <= to_free) {
+    dt = to_col;
+    if (gas_next) {
+      p.coll = 'G';
+      p.n_coll += 1;
+      p.next_gas = xadd(p.next_gas, rng_exponential(p.rng, P.tc));
+    } else {
+      p.n_bounce += 1;
+      p.coll = 'W';
+    }
+    if (to_col == to_free && window_end) finished = true;
+  } else {
+    p.coll = 'N';
+    dt = to_free;
+    if (window_end) finished = true;
+  }
+  // ---- ballistic move (update_position_and_velocity)
+  s0.t = p.t;
+  s0.px = p.px; s0.py = p.py; s0.pz = p.pz;
+  s0.vx = p.vx; s0.vy = p.vy; s0.vz = p.vz;
+  p.t = xadd(p.t, dt);
+  const double ay = P.gravity ? G : 0.0;
+  const double hax = xmul(xmul(0.5 * 0.0, dt), dt);
+  const double hay = xmul(xmul(0.5 * ay, dt), dt);
+  p.px = xadd(xadd(s0.px, xmul(s0.vx, dt)), hax);
+  p.py = xadd(xadd(s0.py, xmul(s0.vy, dt)), hay);
+  p.pz = xadd(xadd(s0.pz, xmul(s0.vz, dt)), hax);
+  p.vx = xadd(p.vx, xmul(0.0, dt));
+  p.vy = xadd(p.vy, xmul(ay, dt));
+  p.vz = xadd(p.vz, xmul(0.0, dt));
+  const double speed = xsqrt(xadd(xadd(xmul(p.vx, p.vx), xmul(p.vy, p.vy)), xmul(p.vz, p.vz)));
+  if (p.coll == 'W') {
+    const char w = p.wall;
+    const bool sx = (w == 'x' || w == 'a' || w == 'b' || w == 'c');
+    const bool sy = (w == 'y' || w == 'a' || w == 'b' || w == 'd');
+    const bool sz = (w == 'z' || w == 'a' || w == 'c' || w == 'd');
+    if (sx) p.px = p.px < 0.0 ? -xmul(P.Lx, 0.5) : xmul(P.Lx, 0.5);
+    if (sy) p.py = p.py < 0.0 ? -xmul(P.Ly, 0.5) : xmul(P.Ly, 0.5);
+    if (sz) p.pz = p.pz < 0.0 ? -xmul(P.Lz, 0.5) : xmul(P.Lz, 0.5);
+    bool diffuse = false;
+    if (P.diffuse > (double)FLT_MIN) diffuse = rng_uniform(p.rng) < P.diffuse;
+    if (diffuse) {
+      // cosine-law diffuse reflection (src/particle.cpp:309-328)
+      const double phi = acos(xsqrt(rng_uniform(p.rng)));
+      const double theta = xmul(xmul(rng_uniform(p.rng), 2.0), 3.141592653589793);
+      const double cp = cos(phi), sp = sin(phi), ct = cos(theta), stt = sin(theta);
+      if (w == 'x') {
+        p.vx = xmul(xmul(xmul(-1.0, sgn1(p.vx)), speed), cp);
+        p.vy = xmul(xmul(-speed, sp), ct);
+        p.vz = xmul(xmul(speed, sp), stt);
+      } else if (w == 'y') {
+        p.vx = xmul(xmul(speed, sp), ct);
+        p.vy = xmul(xmul(xmul(-1.0, sgn1(p.vy)), speed), cp);
+        p.vz = xmul(xmul(speed, sp), stt);
+      } else if (w == 'z') {
+        p.vx = xmul(xmul(speed, sp), ct);
+        p.vy = xmul(xmul(speed, sp), stt);
+        p.vz = xmul(xmul(xmul(-1.0, sgn1(p.vz)), speed), cp);
+      } else {
+        p.stop = true;  // a diffuse hit on an edge or corner stops the particle
+      }
+    } else {
+      if (sx) p.vx = -p.vx;
+      if (sy) p.vy = -p.vy;
+      if (sz) p.vz = -p.vz;
+    }
+  } else if (p.coll == 'G') {
+    if (P.dist == 'M') {
+      p.vx = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);
+      p.vy = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);
+      p.vz = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);
+    } else if (P.dist == 'C') {
+      const double dx = rng_normal(p.rng, 0.0, 1.0);
+      const double dy = rng_normal(p.rng, 0.0, 1.0);
+      const double dz = rng_normal(p.rng, 0.0, 1.0);
+      const double nrm = xsqrt(xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz)));
+      p.vx = xdiv(xmul(dx, speed), nrm);
+      p.vy = xdiv(xmul(dy, speed), nrm);
+      p.vz = xdiv(xmul(dz, speed), nrm);
+    }
+  }
+  // ---- sanity_check
+  const double tol = 1.0e-15;
+  if (fabs(p.px) > xadd(hLx, tol) || fabs(p.py) > xadd(hLy, tol) || fabs(p.pz) > xadd(hLz, tol)) {
+    p.stop = true; p.fail = 1;  // out of bounds
+  } else if (isinf(s0.t) || isinf(p.t)) {
+    p.stop = true; p.fail = 2;  // infinite time
+  } else if (isnan(s0.px) || isnan(s0.py) || isnan(s0.pz) || isnan(p.px) || isnan(p.py) || isnan(p.pz)) {
+    p.stop = true; p.fail = 3;  // NaN position
+  } else if (isnan(p.vx) || isnan(p.vy) || isnan(p.vz) || isnan(s0.vx) || isnan(s0.vy) || isnan(s0.vz)) {
+    p.stop = true; p.fail = 4;  // NaN velocity
+  }
+  return finished;
+}
+
+// ------------------------------------------------------------ field model
+// Integrator state of the current segment.  Omega(tau) = gamma*B at time
+// t0 + tau is the quadratic o0 + tau*(o1 + tau*o2) (plus the pulse).
+struct Seg {
+  double o0x, o0y, o0z, o1x, o1y, o1z, o2x, o2y, o2z;
+#if !ST_GRAD_IS_LINEAR
+  double p0x, p0y, p0z, v0x, v0y, v0z;
+#endif
+  double gpa;          // gamma * pulse amplitude (0: no pulse)
+  double t0, xf, x, h, posneg, facold;
+  double kx, ky, kz;   // DOP853: derivative at (x, y) (FSAL); RK45: last stage-6 state
+  double lastH, lnprev;
+  unsigned int nstep;
+  bool reject, last;
+};
+
+__device__ __forceinline__ void seg_setup(Seg& g, const SetParams& P, const SegStart& s0, double t_end) {
+  const double gm = P.gamma;
+  const Vec3 p0 = {s0.px, s0.py, s0.pz};
+  const Vec3 v0 = {s0.vx, s0.vy, s0.vz};
+  const double cx = s0.vy * P.Ez - s0.vz * P.Ey;
+  const double cy = s0.vz * P.Ex - s0.vx * P.Ez;
+  const double cz = s0.vx * P.Ey - s0.vy * P.Ex;
+  const double g_ = P.gravity ? kGravity : 0.0;
+#if ST_GRAD_IS_LINEAR
+  const Vec3 Gp = st_grad(p0, P);
+  const Vec3 Gv = st_grad(v0, P);
+  const Vec3 Gy = st_grad(Vec3{0.0, 1.0, 0.0}, P);
+  g.o0x = gm * (P.B0x + Gp.x + P.inv_c2 * cx);
+  g.o0y = gm * (P.B0y + Gp.y + P.inv_c2 * cy);
+  g.o0z = gm * (P.B0z + Gp.z + P.inv_c2 * cz);
+  // d/dtau: grad(v0) and the gravity term of v x E, (g yhat) x E = g (Ez, 0, -Ex)
+  g.o1x = gm * (Gv.x + P.inv_c2 * g_ * P.Ez);
+  g.o1y = gm * (Gv.y);
+  g.o1z = gm * (Gv.z - P.inv_c2 * g_ * P.Ex);
+  g.o2x = gm * (0.5 * g_ * Gy.x);
+  g.o2y = gm * (0.5 * g_ * Gy.y);
+  g.o2z = gm * (0.5 * g_ * Gy.z);
+#else
+  g.p0x = p0.x; g.p0y = p0.y; g.p0z = p0.z;
+  g.v0x = v0.x; g.v0y = v0.y; g.v0z = v0.z;
+  g.o0x = gm * (P.B0x + P.inv_c2 * cx);
+  g.o0y = gm * (P.B0y + P.inv_c2 * cy);
+  g.o0z = gm * (P.B0z + P.inv_c2 * cz);
+  g.o1x = gm * (P.inv_c2 * g_ * P.Ez);
+  g.o1y = 0.0;
+  g.o1z = gm * (-P.inv_c2 * g_ * P.Ex);
+  g.o2x = g.o2y = g.o2z = 0.0;
+#endif
+  g.gpa = gm * P.a;
+  g.t0 = s0.t;
+  g.xf = t_end;
+  g.x = s0.t;
+  g.posneg = (t_end - s0.t < 0.0) ? -1.0 : 1.0;
+}
+
+// Omega = gamma * B at tau = t - t0.
+__device__ __forceinline__ void omega_at(const Seg& g, const SetParams& P, double tau, double& Ox, double& Oy,
+                                         double& Oz) {
+  Ox = fma(fma(g.o2x, tau, g.o1x), tau, g.o0x);
+  Oy = fma(fma(g.o2y, tau, g.o1y), tau, g.o0y);
+  Oz = fma(fma(g.o2z, tau, g.o1z), tau, g.o0z);
+#if !ST_GRAD_IS_LINEAR
+  {
+    const double gy = P.gravity ? 0.5 * kGravity : 0.0;
+    const Vec3 pos = {fma(g.v0x, tau, g.p0x), fma(fma(gy, tau, g.v0y), tau, g.p0y), fma(g.v0z, tau, g.p0z)};
+    const Vec3 Gp = st_grad(pos, P);
+    Ox = fma(P.gamma, Gp.x, Ox);
+    Oy = fma(P.gamma, Gp.y, Oy);
+    Oz = fma(P.gamma, Gp.z, Oz);
+  }
+#endif
+#if ST_PULSE_IS_Z_COS
+  if (g.gpa != 0.0) Oz = fma(g.gpa, cos(P.w * (g.t0 + tau)), Oz);
+#else
+  {
+    const Vec3 pu = st_pulse(g.t0 + tau, P);
+    Ox = fma(P.gamma, pu.x, Ox);
+    Oy = fma(P.gamma, pu.y, Oy);
+    Oz = fma(P.gamma, pu.z, Oz);
+  }
+#endif
+}
+
+// Bloch right-hand side f = y x Omega (src/integrator.cpp:83-88).
+__device__ __forceinline__ void bloch(double yx, double yy, double yz, double Ox, double Oy, double Oz, double& fx,
+                                      double& fy, double& fz) {
+  fx = fma(yy, Oz, -yz * Oy);
+  fy = fma(yz, Ox, -yx * Oz);
+  fz = fma(yx, Oy, -yy * Ox);
+}
+
+__device__ __forceinline__ void feval(const Seg& g, const SetParams& P, double tau, double yx, double yy, double yz,
+                                      double& fx, double& fy, double& fz) {
+  double Ox, Oy, Oz;
+  omega_at(g, P, tau, Ox, Oy, Oz);
+  bloch(yx, yy, yz, Ox, Oy, Oz, fx, fy, fz);
+}
+
+// ------------------------------------------------------------ DOP853
+// Start a DOP853 call over the segment (src/integrator.cpp:102-119).
+__device__ __forceinline__ void dop_begin(Seg& g, const SetParams& P, double Sx, double Sy, double Sz, double h) {
+  g.h = h;
+  g.facold = 1.0e-4;
+  g.nstep = 0;
+  g.reject = false;
+  g.last = false;
+  feval(g, P, 0.0, Sx, Sy, Sz, g.kx, g.ky, g.kz);
+}
+
+// One attempted DOP853 step (one pass of the loop at src/integrator.cpp:128-247).
+// Returns 0 to continue, 1 when the segment's last step was accepted (g.h then
+// holds that step, as the reference returns it), -1 after more than nmax
+// attempts.
+__device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz) {
+  using namespace dop;
+  if (g.nstep > P.nmax) return -1;
+  double h = g.h;
+  bool last = g.last;
+  if ((g.x + 1.01 * h - g.xf) * g.posneg > 0.0) {
+    h = g.xf - g.x;
+    last = true;
+  }
+  if (h < P.hmin && !last) h = P.hmin;
+  g.nstep++;
+  const double tx = g.x - g.t0;
+  const double k1x = g.kx, k1y = g.ky, k1z = g.kz;
+  double ax, ay, az, yx, yy, yz;
+#define ST_ACC1(c1, a) ax = (c1) * a##x; ay = (c1) * a##y; az = (c1) * a##z;
+#define ST_ACC(c, a) ax = fma((c), a##x, ax); ay = fma((c), a##y, ay); az = fma((c), a##z, az);
+#define ST_YY() yx = fma(h, ax, Sx); yy = fma(h, ay, Sy); yz = fma(h, az, Sz);
+  double k2x, k2y, k2z, k3x, k3y, k3z, k4x, k4y, k4z, k5x, k5y, k5z, k6x, k6y, k6z;
+  double k7x, k7y, k7z, k8x, k8y, k8z, k9x, k9y, k9z, k10x, k10y, k10z;
+  // stage 2
+  ST_ACC1(A21, k1) ST_YY() feval(g, P, fma(C2, h, tx), yx, yy, yz, k2x, k2y, k2z);
+  // stage 3
+  ST_ACC1(A31, k1) ST_ACC(A32, k2) ST_YY() feval(g, P, fma(C3, h, tx), yx, yy, yz, k3x, k3y, k3z);
+  // stage 4
+  ST_ACC1(A41, k1) ST_ACC(A43, k3) ST_YY() feval(g, P, fma(C4, h, tx), yx, yy, yz, k4x, k4y, k4z);
+  // stage 5
+  ST_ACC1(A51, k1) ST_ACC(A53, k3) ST_ACC(A54, k4) ST_YY() feval(g, P, fma(C5, h, tx), yx, yy, yz, k5x, k5y, k5z);
+  // stage 6
+  ST_ACC1(A61, k1) ST_ACC(A64, k4) ST_ACC(A65, k5) ST_YY() feval(g, P, fma(C6, h, tx), yx, yy, yz, k6x, k6y, k6z);
+  // stage 7
+  ST_ACC1(A71, k1) ST_ACC(A74, k4) ST_ACC(A75, k5) ST_ACC(A76, k6) ST_YY()
+  feval(g, P, fma(C7, h, tx), yx, yy, yz, k7x, k7y, k7z);
+  // stage 8
+  ST_ACC1(A81, k1) ST_ACC(A84, k4) ST_ACC(A85, k5) ST_ACC(A86, k6) ST_ACC(A87, k7) ST_YY()
+  feval(g, P, fma(C8, h, tx), yx, yy, yz, k8x, k8y, k8z);
+  // stage 9
+  ST_ACC1(A91, k1) ST_ACC(A94, k4) ST_ACC(A95, k5) ST_ACC(A96, k6) ST_ACC(A97, k7) ST_ACC(A98, k8) ST_YY()
+  feval(g, P, fma(C9, h, tx), yx, yy, yz, k9x, k9y, k9z);
+  // stage 10
+  ST_ACC1(A101, k1) ST_ACC(A104, k4) ST_ACC(A105, k5) ST_ACC(A106, k6) ST_ACC(A107, k7) ST_ACC(A108, k8)
+  ST_ACC(A109, k9) ST_YY()
+  feval(g, P, fma(C10, h, tx), yx, yy, yz, k10x, k10y, k10z);
+  // stage 11 (result in k2, which is no longer needed)
+  ST_ACC1(A111, k1) ST_ACC(A114, k4) ST_ACC(A115, k5) ST_ACC(A116, k6) ST_ACC(A117, k7) ST_ACC(A118, k8)
+  ST_ACC(A119, k9) ST_ACC(A1110, k10) ST_YY()
+  feval(g, P, fma(C11, h, tx), yx, yy, yz, k2x, k2y, k2z);
+  // stage 12 at x + h (result in k3); its Omega is reused for the FSAL derivative
+  ST_ACC1(A121, k1) ST_ACC(A124, k4) ST_ACC(A125, k5) ST_ACC(A126, k6) ST_ACC(A127, k7) ST_ACC(A128, k8)
+  ST_ACC(A129, k9) ST_ACC(A1210, k10) ST_ACC(A1211, k2) ST_YY()
+  const double tph = tx + h;
+  double Ox12, Oy12, Oz12;
+  omega_at(g, P, tph, Ox12, Oy12, Oz12);
+  bloch(yx, yy, yz, Ox12, Oy12, Oz12, k3x, k3y, k3z);
+  // 8th-order combination and the new state
+  ST_ACC1(B1, k1) ST_ACC(B6, k6) ST_ACC(B7, k7) ST_ACC(B8, k8) ST_ACC(B9, k9) ST_ACC(B10, k10) ST_ACC(B11, k2)
+  ST_ACC(B12, k3)
+  const double bx = ax, by = ay, bz = az;
+  const double nx = fma(h, bx, Sx), ny = fma(h, by, Sy), nz = fma(h, bz, Sz);
+  // error estimates: 3rd-order (bhh) and 5th-order (er) rows
+  const double e1x = fma(-BHH3, k3x, fma(-BHH2, k9x, fma(-BHH1, k1x, bx)));
+  const double e1y = fma(-BHH3, k3y, fma(-BHH2, k9y, fma(-BHH1, k1y, by)));
+  const double e1z = fma(-BHH3, k3z, fma(-BHH2, k9z, fma(-BHH1, k1z, bz)));
+  ST_ACC1(ER1, k1) ST_ACC(ER6, k6) ST_ACC(ER7, k7) ST_ACC(ER8, k8) ST_ACC(ER9, k9) ST_ACC(ER10, k10) ST_ACC(ER11, k2)
+  ST_ACC(ER12, k3)
+#undef ST_ACC1
+#undef ST_ACC
+#undef ST_YY
+  const double wx = rcp_full(fma(P.rtol, max_d(fabs(Sx), fabs(nx)), P.atol));
+  const double wy = rcp_full(fma(P.rtol, max_d(fabs(Sy), fabs(ny)), P.atol));
+  const double wz = rcp_full(fma(P.rtol, max_d(fabs(Sz), fabs(nz)), P.atol));
+  const double q1x = e1x * wx, q1y = e1y * wy, q1z = e1z * wz;
+  const double q2x = ax * wx, q2y = ay * wy, q2z = az * wz;
+  const double err2 = fma(q1z, q1z, fma(q1y, q1y, q1x * q1x));
+  double err = fma(q2z, q2z, fma(q2y, q2y, q2x * q2x));
+  double deno = fma(0.01, err2, err);
+  if (deno <= 0.0) deno = 1.0;
+  err = (fabs(h) * err) * rsqrt_full(deno * 3.0);
+  // step-size controller (Lund-stabilised, clamped to [1/fac2, 1/fac1])
+  double hnew;
+  const bool fast = (P.beta == 0.0) && (err > 1e-300) && (err < 1e300);
+  double rr = 0.0, fac11 = 0.0;
+  if (fast) {
+    rr = rroot8(err);  // 1 / fac11
+    hnew = h * min_d(P.fac2, max_d(P.fac1, P.safe * rr));
+  } else {
+    fac11 = pow(err, P.expo1);
+    double fac = fac11 / pow(g.facold, P.beta);
+    fac = max_d(P.facc2, min_d(P.facc1, fac / P.safe));
+    hnew = h / fac;
+  }
+  int ret = 0;
+  if (err <= 1.0 || P.fixed) {
+    g.facold = max_d(err, 1.0e-4);
+    bloch(nx, ny, nz, Ox12, Oy12, Oz12, g.kx, g.ky, g.kz);  // FSAL: f(x + h, y_new)
+    Sx = nx; Sy = ny; Sz = nz;
+    g.x = g.x + h;
+    if (last) {
+      g.h = h;
+      g.last = true;
+      return 1;
+    }
+    if (fabs(hnew) > P.hmax) hnew = g.posneg * P.hmax;
+    if (g.reject) hnew = g.posneg * min_d(fabs(hnew), fabs(h));
+    g.reject = false;
+  } else {
+    hnew = fast ? h * max_d(P.fac1, P.safe * rr) : h / min_d(P.facc1, fac11 / P.safe);
+    g.reject = true;
+    last = false;
+  }
+  g.last = last;
+  g.h = P.fixed ? h : hnew;
+  return ret;
+}
+
+// ------------------------------------------------------------ RK45
+__device__ __forceinline__ void rk45_begin(Seg& g, double h) {
+  g.h = h;
+  g.lastH = h;
+  g.lnprev = 0.0;  // log(prev_ratio = 1)
+  g.kx = g.ky = g.kz = 0.0;  // the stage state a fresh call starts from
+  g.nstep = 0;
+  g.last = false;
+}
+
+// One attempt of integrateRK45 (src/integrator.cpp:267-335), including its
+// first-stage quirk: k1 is evaluated at the previous attempt's last stage
+// state (zero on the first attempt of a call).  Returns 0 to continue, 1 when
+// the segment end was reached (g.h then holds the carried step), -1 when
+// h < hmin, -2 after more than nmax attempts.
+__device__ __forceinline__ int rk45_attempt(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz) {
+  using namespace rk45;
+  g.nstep++;
+  if (g.nstep > P.nmax) return -2;
+  const double endDt = g.xf - g.x;
+  double h = g.h;
+  g.lastH = h;
+  if (P.fixed) {
+    h = P.h0;
+  } else {
+    if (h > P.hmax)
+      h = std_min(h, P.hmax);
+    else if (h < P.hmin)
+      return -1;
+  }
+  bool stop;
+  if (h >= endDt) {
+    h = endDt;
+    stop = true;
+  } else {
+    g.lastH = h;
+    stop = false;
+  }
+  const double tx = g.x - g.t0;
+  double k1x, k1y, k1z, k2x, k2y, k2z, k3x, k3y, k3z, k4x, k4y, k4z, k5x, k5y, k5z, k6x, k6y, k6z;
+  double yx, yy, yz;
+  feval(g, P, tx, g.kx, g.ky, g.kz, k1x, k1y, k1z);
+  yx = fma(h * B21, k1x, Sx); yy = fma(h * B21, k1y, Sy); yz = fma(h * B21, k1z, Sz);
+  feval(g, P, fma(A2, h, tx), yx, yy, yz, k2x, k2y, k2z);
+  yx = fma(h, fma(B32, k2x, B31 * k1x), Sx);
+  yy = fma(h, fma(B32, k2y, B31 * k1y), Sy);
+  yz = fma(h, fma(B32, k2z, B31 * k1z), Sz);
+  feval(g, P, fma(A3, h, tx), yx, yy, yz, k3x, k3y, k3z);
+  yx = fma(h, fma(B43, k3x, fma(B42, k2x, B41 * k1x)), Sx);
+  yy = fma(h, fma(B43, k3y, fma(B42, k2y, B41 * k1y)), Sy);
+  yz = fma(h, fma(B43, k3z, fma(B42, k2z, B41 * k1z)), Sz);
+  feval(g, P, fma(A4, h, tx), yx, yy, yz, k4x, k4y, k4z);
+  yx = fma(h, fma(B54, k4x, fma(B53, k3x, fma(B52, k2x, B51 * k1x))), Sx);
+  yy = fma(h, fma(B54, k4y, fma(B53, k3y, fma(B52, k2y, B51 * k1y))), Sy);
+  yz = fma(h, fma(B54, k4z, fma(B53, k3z, fma(B52, k2z, B51 * k1z))), Sz);
+  feval(g, P, fma(A5, h, tx), yx, yy, yz, k5x, k5y, k5z);
+  yx = fma(h, fma(B65, k5x, fma(B64, k4x, fma(B63, k3x, fma(B62, k2x, B61 * k1x)))), Sx);
+  yy = fma(h, fma(B65, k5y, fma(B64, k4y, fma(B63, k3y, fma(B62, k2y, B61 * k1y)))), Sy);
+  yz = fma(h, fma(B65, k5z, fma(B64, k4z, fma(B63, k3z, fma(B62, k2z, B61 * k1z)))), Sz);
+  feval(g, P, fma(A6, h, tx), yx, yy, yz, k6x, k6y, k6z);
+  g.kx = yx; g.ky = yy; g.kz = yz;  // the next attempt's first stage sees this state
+  // CH2 and CT2 are zero: k2 does not enter the weights
+  const double wx = fma(CH6, k6x, fma(CH5, k5x, fma(CH4, k4x, fma(CH3, k3x, CH1 * k1x))));
+  const double wy = fma(CH6, k6y, fma(CH5, k5y, fma(CH4, k4y, fma(CH3, k3y, CH1 * k1y))));
+  const double wz = fma(CH6, k6z, fma(CH5, k5z, fma(CH4, k4z, fma(CH3, k3z, CH1 * k1z))));
+  const double tex = h * fma(CT6, k6x, fma(CT5, k5x, fma(CT4, k4x, fma(CT3, k3x, CT1 * k1x))));
+  const double tey = h * fma(CT6, k6y, fma(CT5, k5y, fma(CT4, k4y, fma(CT3, k3y, CT1 * k1y))));
+  const double tez = h * fma(CT6, k6z, fma(CT5, k5z, fma(CT4, k4z, fma(CT3, k3z, CT1 * k1z))));
+  double error = sqrt(fma(tez, tez, fma(tey, tey, tex * tex)));
+  error = std_max(error, 1.0e-16);
+  const double ratio = P.rtol / error;
+  const double lnr = log(ratio);
+  double q = exp(E1 * lnr + E2 * g.lnprev);  // ratio^E1 * prev_ratio^E2
+  q = std_min(q, 4.0);
+  if ((q > 0.81 && error < 2.0 * P.rtol) || P.fixed) {
+    Sx = fma(h, wx, Sx); Sy = fma(h, wy, Sy); Sz = fma(h, wz, Sz);
+    g.x += h;
+    if (stop) {
+      g.h = g.lastH;
+      return 1;
+    }
+  }
+  g.h = P.fixed ? h : h * q;
+  g.lnprev = lnr;
+  return 0;
+}
+
+}  // namespace st

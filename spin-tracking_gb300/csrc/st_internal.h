@@ -1,0 +1,101 @@
+// Internal types shared by the host library (st_api.cpp) and the kernels
+// (st_kernels.cu).  Not part of the public ABI (include/spintrack.h).
+#pragma once
+
+#include <stdint.h>
+#include "spintrack.h"
+
+namespace st {
+
+// Trajectory / integrator constants of the reference (include/options.h:7-8).
+constexpr double kGravity = -9.81;
+constexpr double kC2 = 299792458.0 * 299792458.0;
+
+// One parameter set, laid out for the device.  Derived once on the host from
+// an st_options; every kernel reads it through a pointer into a device table
+// (broadcast loads for a single-set run, per-lane loads in batched runs).
+struct SetParams {
+  // ---- trajectory (src/particle.cpp:121-444)
+  double Lx, Ly, Lz;              // box edges
+  double maxPosStep, tc, sqrtKT_m, diffuse, V;
+  // ---- spin field (src/integrator.cpp:40-88)
+  double gamma;
+  double B0x, B0y, B0z, Ex, Ey, Ez;
+  double Gx[3], Gy[3], Gz[3];     // rows: B_i = dot(pos, G_i)
+  double a, w;                    // pulse amplitude and angular frequency
+  double inv_c2;                  // 1.0 / c^2 as the reference evaluates it
+  // ---- stepper (src/integrator.cpp:90-337)
+  double rtol, atol, hmin, hmax, h0, safe, fac1, fac2, beta;
+  double facc1, facc2, expo1, inv_safe;
+  // ---- windows (src/simulation.cpp:43-49)
+  double t0, tf, ioutInt;
+  double yi_x, yi_y, yi_z;
+  unsigned int nmax, seed;
+  int integrator;                 // 0 DOP853, 1 RK45, any other value: trajectory only
+  int nwin;                       // floor((tf - t0) / ioutInt)
+  int gravity, gas, fixed, keep;
+  int dist;                       // 'C' or 'M'
+  int64_t first;                  // global index of the set's first particle
+  int64_t n;                      // particles in the set
+};
+
+// Device SoA particle state.  RNG state and bookkeeping live beside the
+// physical state so a particle can be resumed from memory at any window end.
+struct DeviceState {
+  int64_t n;
+  double *t, *px, *py, *pz, *vx, *vy, *vz, *Sx, *Sy, *Sz, *h, *next_gas;
+  uint64_t *rx, *ry, *rz, *rw;    // xoshiro words
+  double *rspare;                 // cached second normal
+  uint8_t *rhas;                  // spare valid
+  int32_t *fail;
+  uint64_t *n_coll, *n_bounce, *n_steps;
+  uint8_t *stop, *coll, *wall;
+  int32_t *set;                   // parameter set of each particle
+  int32_t *w_done;                // windows completed
+};
+
+// Snapshot block: 14 field arrays over all particles, each padded to 256 B.
+struct SnapLayout {
+  int64_t n;
+  size_t off[14];
+  size_t bytes;
+};
+
+// Device-side run counters and status (one per context).
+struct RunStatus {
+  unsigned long long dop_attempts;
+  unsigned long long rk45_attempts;
+  unsigned long long segments;
+  unsigned long long queue_head;   // persistent-kernel work queue cursor
+  unsigned long long deadline_ns;  // %globaltimer value after which lanes stop (0 = none)
+  int deadline_hit;
+  int pad;
+};
+
+struct RunArgs {
+  const SetParams* sets;
+  int nsets;
+  const int64_t* order;           // work order (persistent kernel), may be null
+  DeviceState s;
+  RunStatus* status;
+  char* snap;                     // snapshot buffer base (device), may be null
+  SnapLayout snap_layout;
+  int w_begin, w_end;             // window range of this call
+  int deadline_armed;             // read RunStatus::deadline_ns at kernel start
+  int count_work;                 // accumulate attempt counters
+};
+
+// Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
+// cast to int (0 = success).
+int launch_init(const RunArgs& a, int block, void* stream);
+int launch_plain_window(const RunArgs& a, int window, int block, void* stream);
+int launch_pack_snapshot(const RunArgs& a, int slot, void* stream);
+int launch_persistent(const RunArgs& a, int variant, int blocks, int block, void* stream);
+int launch_until(const RunArgs& a, double next_t, int block, void* stream);
+int launch_arm_deadline(RunStatus* status, unsigned long long budget_ns, void* stream);
+int probe_fp64(int sm_count, int iters, double* seconds, double* flops);
+int persistent_variant_count();
+int persistent_max_blocks_per_sm(int variant, int block);
+const char* persistent_variant_name(int variant);
+
+}  // namespace st

@@ -1,0 +1,430 @@
+// Kernels of the hot path and their launch helpers.
+//
+//  k_init        initParticles: seed + position + velocity + gas clock, one
+//                thread per particle (src/particle.cpp:638-710).
+//  k_plain       runSimulation(nextTOut): one thread per particle advances its
+//                particle to the window end with the reference's nested loops
+//                (segment loop, step loop), one launch per output window
+//                (src/particle.cpp:525-635, 865-876).
+//  k_persistent  the batched engine: a persistent grid whose lanes pull
+//                particles (of any parameter set) from a device work queue and
+//                run them through all requested windows.  The per-lane loop is
+//                flattened so that every iteration performs exactly one step
+//                attempt: a lane whose segment ended does its trajectory event
+//                and joins the next attempt, and a lane whose particle finished
+//                takes the next particle, so warps stay converged on the step
+//                code.  Snapshots go straight to the snapshot buffer.
+//  k_pack        copies the state into one snapshot block (plain path).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "st_device.cuh"
+
+namespace st {
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Deadline armed for this run (0 = none); read once per thread.
+__device__ __forceinline__ unsigned long long run_deadline(const RunArgs& a) {
+  return a.deadline_armed ? *((volatile unsigned long long*)&a.status->deadline_ns) : 0ull;
+}
+__device__ __forceinline__ bool past_deadline(unsigned long long dl) { return dl != 0ull && globaltimer_ns() > dl; }
+
+__global__ void k_arm(RunStatus* st, unsigned long long budget_ns) { st->deadline_ns = globaltimer_ns() + budget_ns; }
+
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+__device__ __forceinline__ void nan_fill(PState& p) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  p.t = nan;
+  p.px = p.py = p.pz = nan;
+  p.vx = p.vy = p.vz = nan;
+  p.Sx = p.Sy = p.Sz = nan;
+}
+
+__device__ __forceinline__ void write_snap(const RunArgs& a, int64_t i, int w, const PState& p) {
+  if (a.snap == nullptr || w < a.w_begin || w >= a.w_end) return;
+  char* b = a.snap + (size_t)(w - a.w_begin) * a.snap_layout.bytes;
+  const size_t* o = a.snap_layout.off;
+  reinterpret_cast<double*>(b + o[0])[i] = p.t;
+  reinterpret_cast<double*>(b + o[1])[i] = p.px;
+  reinterpret_cast<double*>(b + o[2])[i] = p.py;
+  reinterpret_cast<double*>(b + o[3])[i] = p.pz;
+  reinterpret_cast<double*>(b + o[4])[i] = p.vx;
+  reinterpret_cast<double*>(b + o[5])[i] = p.vy;
+  reinterpret_cast<double*>(b + o[6])[i] = p.vz;
+  reinterpret_cast<double*>(b + o[7])[i] = p.Sx;
+  reinterpret_cast<double*>(b + o[8])[i] = p.Sy;
+  reinterpret_cast<double*>(b + o[9])[i] = p.Sz;
+  reinterpret_cast<int32_t*>(b + o[10])[i] = p.fail;
+  reinterpret_cast<uint64_t*>(b + o[11])[i] = p.n_coll;
+  reinterpret_cast<uint64_t*>(b + o[12])[i] = p.n_bounce;
+  reinterpret_cast<uint64_t*>(b + o[13])[i] = p.n_steps;
+}
+
+// ------------------------------------------------------------------ init
+__global__ void k_init(RunArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.s.n) return;
+  const SetParams& P = a.sets[a.s.set[i]];
+  const PState p = init_particle(P, (unsigned int)(i - P.first));
+  store_state(a.s, i, p);
+  a.s.w_done[i] = 0;
+}
+
+// ------------------------------------------------------------------ plain
+// The reference's per-particle window loop (src/particle.cpp:558-614) with
+// nested segment and step loops.  Returns false if the deadline passed (the
+// caller then discards the window's progress).
+__device__ __forceinline__ bool window_nested(PState& p, const SetParams& P, double tf, unsigned long long dl,
+                                              unsigned long long& n_dop, unsigned long long& n_rk,
+                                              unsigned long long& n_seg) {
+  double tempH = p.h;
+  bool finished = false;
+  unsigned int guard = 0;
+  while (!finished && !p.stop) {
+    SegStart s0;
+    finished = traj_event(p, P, tf, s0);
+    ++n_seg;
+    if (p.fail == 0) {
+      int res = 0;
+      if (P.integrator == 0 || P.integrator == 1) {
+        Seg g;
+        seg_setup(g, P, s0, p.t);
+        if (P.integrator == 0) {
+          dop_begin(g, P, p.Sx, p.Sy, p.Sz, tempH);
+          do {
+            res = dop_attempt(g, P, p.Sx, p.Sy, p.Sz);
+            ++n_dop;
+            if (((++guard) & 1023u) == 0u && past_deadline(dl)) return false;
+          } while (res == 0);
+        } else {
+          rk45_begin(g, tempH);
+          do {
+            res = rk45_attempt(g, P, p.Sx, p.Sy, p.Sz);
+            ++n_rk;
+            if (((++guard) & 1023u) == 0u && past_deadline(dl)) return false;
+          } while (res == 0);
+        }
+        tempH = g.h;
+        if (res > 0) res = 0;
+      }
+      if (P.keep) p.h = tempH;
+      if (res < 0) {
+        p.stop = true;
+        p.fail = res;
+      }
+    }
+    if (p.stop) nan_fill(p);
+    p.n_steps += 1;
+    if (((++guard) & 255u) == 0u && past_deadline(dl)) return false;
+  }
+  return true;
+}
+
+// window >= 0: advance particles whose next window is `window` to its end
+// ((window+1)*ioutInt of their set) and mark it done.  window < 0: advance
+// every particle to next_t (runSimulation semantics, no window bookkeeping).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_plain(RunArgs a, int window, double next_t) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long n_dop = 0, n_rk = 0, n_seg = 0;
+  bool hit = false;
+  const unsigned long long dl = run_deadline(a);
+  if (i < a.s.n) {
+    const SetParams& P = a.sets[a.s.set[i]];
+    double tf = next_t;
+    bool run = true;
+    if (window >= 0) {
+      run = window < P.nwin && a.s.w_done[i] == window;
+      tf = ((double)window + 1.0) * P.ioutInt;
+    }
+    if (run) {
+      PState p = load_state(a.s, i);
+      if (window_nested(p, P, tf, dl, n_dop, n_rk, n_seg)) {
+        store_state(a.s, i, p);
+        if (window >= 0) a.s.w_done[i] = window + 1;
+      } else {
+        hit = true;
+      }
+    }
+  }
+  if (hit) atomicExch(&a.status->deadline_hit, 1);
+  if (a.count_work) {
+    warp_add(&a.status->dop_attempts, n_dop);
+    warp_add(&a.status->rk45_attempts, n_rk);
+    warp_add(&a.status->segments, n_seg);
+  }
+}
+
+// ------------------------------------------------------------------ pack
+__global__ void k_pack(RunArgs a, int slot) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.s.n) return;
+  char* b = a.snap + (size_t)slot * a.snap_layout.bytes;
+  const size_t* o = a.snap_layout.off;
+  reinterpret_cast<double*>(b + o[0])[i] = a.s.t[i];
+  reinterpret_cast<double*>(b + o[1])[i] = a.s.px[i];
+  reinterpret_cast<double*>(b + o[2])[i] = a.s.py[i];
+  reinterpret_cast<double*>(b + o[3])[i] = a.s.pz[i];
+  reinterpret_cast<double*>(b + o[4])[i] = a.s.vx[i];
+  reinterpret_cast<double*>(b + o[5])[i] = a.s.vy[i];
+  reinterpret_cast<double*>(b + o[6])[i] = a.s.vz[i];
+  reinterpret_cast<double*>(b + o[7])[i] = a.s.Sx[i];
+  reinterpret_cast<double*>(b + o[8])[i] = a.s.Sy[i];
+  reinterpret_cast<double*>(b + o[9])[i] = a.s.Sz[i];
+  reinterpret_cast<int32_t*>(b + o[10])[i] = a.s.fail[i];
+  reinterpret_cast<uint64_t*>(b + o[11])[i] = a.s.n_coll[i];
+  reinterpret_cast<uint64_t*>(b + o[12])[i] = a.s.n_bounce[i];
+  reinterpret_cast<uint64_t*>(b + o[13])[i] = a.s.n_steps[i];
+}
+
+// ------------------------------------------------------------------ persistent
+enum LaneMode { M_FETCH = 0, M_EVENT = 1, M_SEG = 2, M_WEND = 3, M_DONE = 4 };
+
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_persistent(RunArgs a) {
+  int mode = M_FETCH;
+  int64_t i = 0;
+  const SetParams* P = a.sets;
+  PState p;
+  Seg g;
+  int w = 0, wlast = 0;
+  double tf = 0.0, tempH = 0.0;
+  bool finished = false, hit = false;
+  unsigned long long n_dop = 0, n_rk = 0, n_seg = 0;
+  unsigned int tick = 0;
+  const unsigned long long dl = run_deadline(a);
+  while (true) {
+    // Phase A (divergent, short): bring this lane to a segment that needs
+    // step attempts, or run out of work.
+    while (mode != M_SEG && mode != M_DONE) {
+      if (mode == M_FETCH) {
+        const unsigned long long item = atomicAdd(&a.status->queue_head, 1ull);
+        if (item >= (unsigned long long)a.s.n) {
+          mode = M_DONE;
+          break;
+        }
+        i = a.order ? a.order[item] : (int64_t)item;
+        P = &a.sets[a.s.set[i]];
+        w = a.s.w_done[i];
+        wlast = min(a.w_end, P->nwin);
+        if (w >= wlast) continue;
+        p = load_state(a.s, i);
+        tf = ((double)w + 1.0) * P->ioutInt;
+        tempH = p.h;
+        finished = false;
+        mode = M_EVENT;
+      }
+      if (mode == M_EVENT) {
+        if (p.stop) {
+          mode = M_WEND;
+        } else {
+          SegStart s0;
+          finished = traj_event(p, *P, tf, s0);
+          ++n_seg;
+          if (p.fail == 0 && (P->integrator == 0 || P->integrator == 1)) {
+            seg_setup(g, *P, s0, p.t);
+            if (P->integrator == 0)
+              dop_begin(g, *P, p.Sx, p.Sy, p.Sz, tempH);
+            else
+              rk45_begin(g, tempH);
+            mode = M_SEG;
+          } else {
+            if (p.fail == 0 && P->keep) p.h = tempH;
+            if (p.stop) nan_fill(p);
+            p.n_steps += 1;
+            mode = (finished || p.stop) ? M_WEND : M_EVENT;
+          }
+          if (((++tick) & 255u) == 0u && past_deadline(dl)) {
+            hit = true;
+            mode = M_DONE;
+            break;
+          }
+        }
+      }
+      if (mode == M_WEND) {
+        write_snap(a, i, w, p);
+        ++w;
+        store_state(a.s, i, p);  // every window end is a resumable checkpoint
+        a.s.w_done[i] = w;
+        if (w < wlast) {
+          tf = ((double)w + 1.0) * P->ioutInt;
+          tempH = p.h;
+          finished = false;
+          mode = M_EVENT;
+        } else {
+          mode = M_FETCH;
+        }
+      }
+    }
+    if (mode == M_DONE) break;
+    // Phase B (converged): one step attempt for every lane.
+    int r;
+    if (P->integrator == 0) {
+      r = dop_attempt(g, *P, p.Sx, p.Sy, p.Sz);
+      ++n_dop;
+    } else {
+      r = rk45_attempt(g, *P, p.Sx, p.Sy, p.Sz);
+      ++n_rk;
+    }
+    if (r != 0) {
+      tempH = g.h;
+      if (P->keep) p.h = tempH;
+      if (r < 0) {
+        p.stop = true;
+        p.fail = r;
+      }
+      if (p.stop) nan_fill(p);
+      p.n_steps += 1;
+      mode = (finished || p.stop) ? M_WEND : M_EVENT;
+    }
+    if (((++tick) & 255u) == 0u && past_deadline(dl)) {
+      hit = true;
+      break;
+    }
+  }
+  if (hit) atomicExch(&a.status->deadline_hit, 1);
+  if (a.count_work) {
+    // lanes leave the loop at different times: aggregate with plain atomics
+    if (n_dop) atomicAdd(&a.status->dop_attempts, n_dop);
+    if (n_rk) atomicAdd(&a.status->rk45_attempts, n_rk);
+    if (n_seg) atomicAdd(&a.status->segments, n_seg);
+  }
+}
+
+// ------------------------------------------------------------------ FP64 peak probe
+// Eight independent DFMA chains per thread: the FP64 pipe's issue rate, the
+// denominator of the step kernels' roofline.
+__global__ void k_fp64_probe(double* out, int iters, double b, double c) {
+  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6,
+         a7 = a0 + 7;
+  for (int k = 0; k < iters; ++k) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  const double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+int probe_fp64(int sm_count, int iters, double* seconds, double* flops) {
+  double* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(double));
+  if (e) return (int)e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sm_count * 8, threads = 256;
+  k_fp64_probe<<<blocks, threads>>>(d, 64, 0.9999999, 1e-7);  // warm-up
+  cudaEventRecord(e0);
+  k_fp64_probe<<<blocks, threads>>>(d, iters, 0.9999999, 1e-7);
+  cudaEventRecord(e1);
+  e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  *seconds = ms * 1e-3;
+  *flops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  return e ? (int)e : (int)cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ launchers
+static inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+
+int launch_init(const RunArgs& a, int block, void* stream) {
+  if (a.s.n == 0) return 0;
+  k_init<<<grid_for(a.s.n, block), block, 0, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+template <int B>
+static int plain_launch(const RunArgs& a, int window, double next_t, void* stream) {
+  k_plain<B><<<grid_for(a.s.n, B), B, 0, (cudaStream_t)stream>>>(a, window, next_t);
+  return (int)cudaGetLastError();
+}
+
+static int plain_dispatch(const RunArgs& a, int window, double next_t, int block, void* stream) {
+  if (a.s.n == 0) return 0;
+  // numPerGPUBlock of the reference picks the block; round to a compiled size
+  if (block <= 32) return plain_launch<32>(a, window, next_t, stream);
+  if (block <= 64) return plain_launch<64>(a, window, next_t, stream);
+  if (block <= 128) return plain_launch<128>(a, window, next_t, stream);
+  return plain_launch<256>(a, window, next_t, stream);
+}
+
+int launch_plain_window(const RunArgs& a, int window, int block, void* stream) {
+  return plain_dispatch(a, window, 0.0, block, stream);
+}
+
+int launch_until(const RunArgs& a, double next_t, int block, void* stream) {
+  return plain_dispatch(a, -1, next_t, block, stream);
+}
+
+int launch_arm_deadline(RunStatus* status, unsigned long long budget_ns, void* stream) {
+  k_arm<<<1, 1, 0, (cudaStream_t)stream>>>(status, budget_ns);
+  return (int)cudaGetLastError();
+}
+
+int launch_pack_snapshot(const RunArgs& a, int slot, void* stream) {
+  if (a.s.n == 0) return 0;
+  k_pack<<<grid_for(a.s.n, 256), 256, 0, (cudaStream_t)stream>>>(a, slot);
+  return (int)cudaGetLastError();
+}
+
+// Persistent-kernel variants: (block threads, min resident blocks per SM).
+// The second number sets the register budget the compiler may use.
+struct Variant {
+  int block, minb;
+  const char* name;
+};
+static const Variant kVariants[] = {
+    {128, 1, "b128_m1"}, {128, 2, "b128_m2"}, {128, 3, "b128_m3"}, {64, 4, "b64_m4"}, {256, 1, "b256_m1"},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+int persistent_variant_count() { return kNumVariants; }
+const char* persistent_variant_name(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "?"; }
+
+template <int B, int M>
+static const void* persistent_fn() {
+  return reinterpret_cast<const void*>(&k_persistent<B, M>);
+}
+static const void* variant_fn(int v) {
+  switch (v) {
+    case 0: return persistent_fn<128, 1>();
+    case 1: return persistent_fn<128, 2>();
+    case 2: return persistent_fn<128, 3>();
+    case 3: return persistent_fn<64, 4>();
+    default: return persistent_fn<256, 1>();
+  }
+}
+
+int persistent_max_blocks_per_sm(int v, int block) {
+  int nb = 0;
+  if (v < 0 || v >= kNumVariants) return 0;
+  if (block <= 0) block = kVariants[v].block;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, variant_fn(v), block, 0);
+  return nb;
+}
+
+int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stream) {
+  if (a.s.n == 0) return 0;
+  if (v < 0 || v >= kNumVariants) return (int)cudaErrorInvalidValue;
+  (void)block;
+  const int b = kVariants[v].block;
+  RunArgs args = a;
+  void* params[] = {&args};
+  cudaError_t e = cudaLaunchKernel(variant_fn(v), dim3(blocks), dim3(b), params, 0, (cudaStream_t)stream);
+  return (int)e;
+}
+
+}  // namespace st

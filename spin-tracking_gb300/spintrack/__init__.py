@@ -1,0 +1,199 @@
+"""spintrack — Python front-end of the GB300 spin-tracking engine.
+
+Mirrors the reference's host interface for the hot path:
+  optionParser / parseLine  -> parse_params / parse_line
+  class particle            -> Particles (init_particles, run_simulation,
+                               output_data), plus the batched window driver
+  mainAnalysis              -> main_analysis (writes output format 'A')
+Every computation runs in libspintrack.so on the GPU (no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from pathlib import Path
+from typing import Iterable
+
+import numpy as np
+
+from . import build
+from ._capi import (KERNEL_PERSISTENT, KERNEL_PLAIN, ST_ERR_DEADLINE, Counters, DeviceSoA, LaunchConfig, Options,
+                    SpinTrackError, StateView, Vec3, check, load)
+from .formats import read_format_a, snapshot_dtype
+
+__all__ = [
+    "Options", "Vec3", "Particles", "SpinTrackError", "default_options", "parse_params", "parse_line",
+    "derive", "num_windows", "make_options", "main_analysis", "read_format_a", "KERNEL_PLAIN",
+    "KERNEL_PERSISTENT", "SNAP_FIELDS",
+]
+
+SNAP_FIELDS = ("t", "pos_x", "pos_y", "pos_z", "v_x", "v_y", "v_z", "S_x", "S_y", "S_z", "fail", "n_coll",
+               "n_bounce", "n_steps")
+_SNAP_DTYPES = (np.float64,) * 10 + (np.int32, np.uint64, np.uint64, np.uint64)
+
+
+def default_options() -> Options:
+    """options{} defaults (include/options.h:10-61)."""
+    o = Options()
+    load().st_options_default(ctypes.byref(o))
+    return o
+
+
+def parse_line(opt: Options, line: str) -> int:
+    """parseLine (src/optionsParser.cpp:40-175): 0 applied, 1 unrecognised key."""
+    return check(load().st_parse_line(ctypes.byref(opt), line.encode()))
+
+
+def parse_params(path: str | Path) -> Options:
+    """optionParser (src/optionsParser.cpp:177-197)."""
+    o = Options()
+    rc = load().st_parse_params(str(path).encode(), ctypes.byref(o))
+    if rc not in (0, -4):  # a missing file keeps the defaults, as the reference does
+        check(rc)
+    return o
+
+
+def derive(opt: Options) -> Options:
+    """tc and sqrtKT_m as mainAnalysis derives them (src/simulation.cpp:9-11)."""
+    load().st_derive(ctypes.byref(opt))
+    return opt
+
+
+def num_windows(opt: Options) -> int:
+    return load().st_num_windows(ctypes.byref(opt))
+
+
+def make_options(**kw) -> Options:
+    """Defaults overridden by keyword values; vectors as 3-sequences, dist as 'C'/'M'."""
+    o = default_options()
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(f"unknown option {k}")
+        cur = getattr(o, k)
+        if isinstance(cur, Vec3):
+            setattr(o, k, Vec3(*map(float, v)))
+        elif k == "dist":
+            o.dist = v.encode() if isinstance(v, str) else v
+        else:
+            setattr(o, k, v)
+    return o
+
+
+class Particles:
+    """The engine object: the reference's `class particle`
+    (include/particle.h:87-314), for one or several parameter sets."""
+
+    def __init__(self, opt: Options | Iterable[Options], device: int = 0, derive_params: bool = False):
+        lib = load()
+        sets = [opt] if isinstance(opt, Options) else list(opt)
+        if derive_params:
+            sets = [derive(Options.from_buffer_copy(bytes(s))) for s in sets]
+        arr = (Options * len(sets))(*sets)
+        self._sets = sets
+        self._ctx = ctypes.c_void_p()
+        check(lib.st_create_batch(arr, len(sets), device, ctypes.byref(self._ctx)))
+        self.n = sum(int(s.numParticles) for s in sets)
+        self.device = device
+
+    # -- reference interface -------------------------------------------
+    def init_particles(self) -> None:
+        """initParticles (include/particle.h:241-252)."""
+        check(load().st_init(self._ctx))
+
+    def run_simulation(self, next_t: float) -> None:
+        """runSimulation(nextTOut) (src/particle.cpp:865-876): plain kernel."""
+        check(load().st_run_until(self._ctx, float(next_t)))
+
+    def output_data(self) -> dict:
+        """outputData (src/particle.cpp:852-862): the snapshot fields as numpy arrays."""
+        n = self.n
+        d = {"t": np.empty(n), "pos": np.empty((n, 3)), "v": np.empty((n, 3)), "S": np.empty((n, 3)),
+             "fail": np.empty(n, np.int32), "n_coll": np.empty(n, np.uint64), "n_bounce": np.empty(n, np.uint64),
+             "n_steps": np.empty(n, np.uint64)}
+        if n == 0:
+            return d
+        P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+        view = StateView(P(d["t"], ctypes.c_double), P(d["pos"], Vec3), P(d["v"], Vec3), P(d["S"], Vec3),
+                         P(d["fail"], ctypes.c_int32), P(d["n_coll"], ctypes.c_uint64),
+                         P(d["n_bounce"], ctypes.c_uint64), P(d["n_steps"], ctypes.c_uint64))
+        check(load().st_read_state(self._ctx, ctypes.byref(view)))
+        return d
+
+    # -- window driver ---------------------------------------------------
+    def run_windows(self, w_begin: int, w_end: int, kernel: int = KERNEL_PERSISTENT, snap_ptr: int = 0) -> int:
+        """Advance windows [w_begin, w_end); snapshot blocks to device pointer snap_ptr (0 = none).
+        Returns 0, or ST_ERR_DEADLINE when the device time budget ran out."""
+        rc = load().st_run_windows(self._ctx, int(kernel), int(w_begin), int(w_end), ctypes.c_void_p(snap_ptr or None))
+        if rc == ST_ERR_DEADLINE:
+            return rc
+        return check(rc)
+
+    def snapshot_bytes(self) -> int:
+        return int(load().st_snapshot_bytes(self._ctx))
+
+    def snapshot_offsets(self) -> list[int]:
+        return [int(load().st_snapshot_field_offset(self._ctx, k)) for k in range(14)]
+
+    def device_state(self) -> DeviceSoA:
+        d = DeviceSoA()
+        check(load().st_device_state(self._ctx, ctypes.byref(d)))
+        return d
+
+    def set_launch_config(self, variant: int = -1, blocks_per_sm: int = 0) -> None:
+        cfg = LaunchConfig(0, int(blocks_per_sm), int(variant))
+        check(load().st_set_launch_config(self._ctx, ctypes.byref(cfg)))
+
+    def launch_config(self) -> tuple[int, int]:
+        cfg = LaunchConfig()
+        check(load().st_get_launch_config(self._ctx, ctypes.byref(cfg)))
+        return cfg.variant, cfg.blocks_per_sm
+
+    def set_deadline(self, seconds: float) -> None:
+        check(load().st_set_deadline(self._ctx, float(seconds)))
+
+    def counters(self) -> dict:
+        c = Counters()
+        check(load().st_get_counters(self._ctx, ctypes.byref(c)))
+        return {k: int(getattr(c, k)) for k, _ in Counters._fields_}
+
+    def synchronize(self) -> None:
+        check(load().st_synchronize(self._ctx))
+
+    def close(self) -> None:
+        if self._ctx:
+            load().st_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def unpack_snapshots(buf: np.ndarray, n: int, offsets: list[int], block_bytes: int, count: int) -> dict:
+    """Split `count` snapshot blocks (raw bytes, host) into per-field arrays [count, n]."""
+    out = {}
+    raw = buf.view(np.uint8)
+    for k, (name, dt) in enumerate(zip(SNAP_FIELDS, _SNAP_DTYPES)):
+        sz = np.dtype(dt).itemsize
+        arr = np.empty((count, n), dtype=dt)
+        for s in range(count):
+            base = s * block_bytes + offsets[k]
+            arr[s] = raw[base:base + sz * n].view(dt)
+        out[name] = arr
+    return out
+
+
+def main_analysis(opt: Options, out_path: str | Path, kernel: int = KERNEL_PERSISTENT, device: int = 0) -> float:
+    """mainAnalysis (src/simulation.cpp:8-96): run and write format 'A'.
+    Returns the wall seconds of the window loop (excluding file writes)."""
+    secs = ctypes.c_double()
+    check(load().st_main_analysis(ctypes.byref(opt), str(out_path).encode(), device, int(kernel), ctypes.byref(secs)))
+    return secs.value

@@ -1,0 +1,213 @@
+"""Pin the oracle (oracle/spin_oracle.c) to the reference.
+
+Every fixture under tests/golden/ was produced by the reference's own sources
+(tests/golden/make_golden.py).  The oracle must reproduce them bit for bit on
+this host (both built with -ffp-contract=off), and it must pass the
+reference's own known-answer tests (tests/integrator_validation.cpp,
+tests/particle_validation.cpp, tests/output_tests.cpp)."""
+from __future__ import annotations
+
+import ctypes
+import math
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GOLDEN_CASES
+from _oracle import Rng, Vec3
+from spintrack.formats import header_equal, read_format_a
+
+
+def hexf(s: str) -> float:
+    return float.fromhex(s)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_format_a_bit_exact(oracle, tmp_path, case):
+    """mainAnalysis end to end: the whole output file equals the reference's."""
+    opt = oracle.parse_file(GOLDEN / f"{case}.params")
+    out = tmp_path / "o.bin"
+    oracle.main_analysis(opt, out, threads=2)
+    a, b = out.read_bytes(), (GOLDEN / f"{case}.bin").read_bytes()
+    assert len(a) == len(b)
+    assert header_equal(a, b)
+    assert a[440:] == b[440:]
+
+
+def _probe_lines(name):
+    return [l.split() for l in (GOLDEN / name).read_text().splitlines() if l.strip()]
+
+
+@pytest.mark.parametrize("dist", ["C", "M"])
+def test_init_matches_reference(oracle, dist):
+    """initParticlesCPU: positions, velocities, gas clock and RNG state."""
+    params = GOLDEN / ("probe.params" if dist == "C" else "probe_m.params")
+    opt = oracle.parse_file(params)
+    p = oracle.alloc(opt.numParticles)
+    oracle.L.or_init(ctypes.byref(opt), ctypes.byref(p), 0)
+    for tok in _probe_lines(f"probe_init_{dist}.txt"):
+        i = int(tok[1])
+        vals = [hexf(x) for x in tok[2:9]]
+        assert [p.pos[i].x, p.pos[i].y, p.pos[i].z] == vals[0:3]
+        assert [p.v[i].x, p.v[i].y, p.v[i].z] == vals[3:6]
+        assert p.next_gas[i] == vals[6]
+        r = p.rng[i]
+        assert [r.x, r.y, r.z, r.w] == [int(x) for x in tok[9:13]]
+        assert int(r.has_spare) == int(tok[13])
+        if r.has_spare:
+            assert r.spare == hexf(tok[14])
+    oracle.free(p)
+
+
+def test_rng_draws_match_reference(oracle):
+    """Raw xoshiro outputs and Marsaglia normals after init."""
+    opt = oracle.parse_file(GOLDEN / "probe.params")
+    p = oracle.alloc(opt.numParticles)
+    oracle.L.or_init(ctypes.byref(opt), ctypes.byref(p), 0)
+    for tok in _probe_lines("probe_draws.txt"):
+        i = int(tok[1])
+        k = (len(tok) - 2) // 2
+        r = Rng.from_buffer_copy(bytes(p.rng[i]))
+        raw = [oracle.L.or_xoshiro(ctypes.byref(r)) for _ in range(k)]
+        assert raw == [int(x) for x in tok[2:2 + k]]
+        nrm = [oracle.L.or_normal(ctypes.byref(r), 0.0, 1.0) for _ in range(k)]
+        assert nrm == [hexf(x) for x in tok[2 + k:]]
+    oracle.free(p)
+
+
+def test_events_match_reference(oracle):
+    """calc_next_collision_time + update_position_and_velocity + sanity_check
+    sequences (gas, diffuse and specular events) for two parameter files."""
+    blocks = (GOLDEN / "probe_events.txt").read_text().split("p 0\n")
+    assert len(blocks) == 3
+    for params, text in zip(["probe.params", "probe_m.params"], blocks[1:]):
+        opt = oracle.parse_file(GOLDEN / params)
+        p = oracle.alloc(opt.numParticles)
+        oracle.L.or_init(ctypes.byref(opt), ctypes.byref(p), 0)
+        i = 0
+        nseg = 0
+        for line in ("p 0\n" + text).splitlines():
+            tok = line.split()
+            if tok[0] == "p":
+                i = int(tok[1])
+                continue
+            oracle.L.or_event(ctypes.byref(opt), ctypes.byref(p), i, opt.tf)
+            ct, wh, stop, fail = tok[1], tok[2], int(tok[3]), int(tok[4])
+            assert p.coll_type[i] == ct.encode()
+            if wh != "-":
+                assert p.wall_hit[i] == wh.encode()
+            assert int(p.stop[i]) == stop and p.fail[i] == fail
+            vals = [hexf(x) for x in tok[5:14]]
+            assert p.t[i] == vals[1]
+            assert [p.pos[i].x, p.pos[i].y, p.pos[i].z] == vals[2:5]
+            assert [p.v[i].x, p.v[i].y, p.v[i].z] == vals[5:8]
+            assert p.next_gas[i] == vals[8]
+            assert p.rng[i].x == int(tok[14])
+            nseg += 1
+        assert nseg > 40
+        oracle.free(p)
+
+
+@pytest.mark.parametrize("which", ["dop", "rk45"])
+def test_segment_steppers_match_reference(oracle, which):
+    """integrateDOP / integrateRK45 over single ballistic segments."""
+    fn = oracle.L.or_integrate_dop if which == "dop" else oracle.L.or_integrate_rk45
+    for line in (GOLDEN / f"probe_{which}.txt").read_text().splitlines():
+        lhs, rhs = line.split("|")
+        a = lhs.split()
+        opt = oracle.parse_file(GOLDEN / a[0])
+        v = [float(x) for x in a[1:]]
+        y = Vec3(*v[2:5])
+        p0 = Vec3(*v[5:8])
+        v0 = Vec3(*v[8:11])
+        h = ctypes.c_double(v[11])
+        ret = fn(ctypes.byref(opt), v[0], v[1], ctypes.byref(y), ctypes.byref(p0), ctypes.byref(v0), ctypes.byref(h))
+        r = rhs.split()
+        assert ret == int(r[1])
+        assert [y.x, y.y, y.z, h.value] == [hexf(x) for x in r[2:6]]
+
+
+def test_free_precession_kat(oracle):
+    """tests/integrator_validation.cpp:12-46: DOP853 free precession about x
+    over [0.1, 1.2] s with rtol = atol = 1e-12 matches the analytic spin to 1e-9."""
+    opt = oracle.default_options()
+    opt.B0 = Vec3(3e-6, 0.0, 0.0)
+    opt.E = Vec3(0.0, 0.0, 0.0)
+    opt.gravity = False
+    opt.rtol = opt.atol = 1e-12
+    y = Vec3(0.0, 0.0, 1.0)
+    z = Vec3(0.0, 0.0, 0.0)
+    h = ctypes.c_double(1e-4)
+    oracle.L.or_integrate_dop(ctypes.byref(opt), 0.1, 1.2, ctypes.byref(y), ctypes.byref(z), ctypes.byref(z),
+                              ctypes.byref(h))
+    ph = 3e-6 * opt.gamma * (1.2 - 0.1)
+    assert abs(y.x) <= 1e-9
+    assert abs(y.y - math.sin(ph)) <= 1e-9
+    assert abs(y.z - math.cos(ph)) <= 1e-9
+
+
+def test_maxwell_boltzmann_init_kat(oracle):
+    """tests/particle_validation.cpp:14-42: loose Maxwell-Boltzmann moments of
+    1e5 initial velocities (T = 0.4 K, m = 1e-26 kg)."""
+    opt = oracle.default_options()
+    opt.gravity = False
+    opt.T = 0.4
+    opt.m = 1e-26
+    opt.dist = b"M"
+    opt.numParticles = 100000
+    k = 1.380649e-23
+    opt.sqrtKT_m = math.sqrt(k * opt.T / opt.m)
+    p = oracle.alloc(opt.numParticles)
+    oracle.L.or_init(ctypes.byref(opt), ctypes.byref(p), 0)
+    v = oracle.arrays(p)["v"]
+    oracle.free(p)
+    s = math.sqrt(k * opt.T / opt.m)
+    assert np.all(np.abs(v.sum(0) / 1e5 / s) < 2e-2)
+    assert abs(math.sqrt((v ** 2).sum() / 1e5) / math.sqrt(3 * k * opt.T / opt.m) - 1) < 2e-2
+
+
+def test_interpolation_kat(oracle):
+    """tests/particle_validation.cpp:44-80: ballistic interpolation with and
+    without gravity."""
+    opt = oracle.default_options()
+    p_old, v_old = Vec3(1, 2, 3), Vec3(1, 2, 3)
+    po, vo = Vec3(), Vec3()
+    opt.gravity = False
+    oracle.L.or_interpolate(ctypes.byref(opt), 1.0, 0.0, ctypes.byref(p_old), ctypes.byref(v_old), ctypes.byref(po),
+                            ctypes.byref(vo))
+    assert (po.x, po.y, po.z, vo.x, vo.y, vo.z) == (2, 4, 6, 1, 2, 3)
+    opt.gravity = True
+    oracle.L.or_interpolate(ctypes.byref(opt), 1.0, 0.0, ctypes.byref(p_old), ctypes.byref(v_old), ctypes.byref(po),
+                            ctypes.byref(vo))
+    g = -9.81
+    assert abs(po.y - (2 + 2 + 0.5 * g)) <= 1e-9 and abs(vo.y - (2 + g)) <= 1e-9
+    assert (po.x, po.z, vo.x, vo.z) == (2, 6, 1, 3)
+
+
+def test_output_test_kat():
+    """tests/output_tests.cpp:20-82 re-expressed on format 'A': snapshot times
+    are i*ioutInt and the spin is free precession at every snapshot (1e-9)."""
+    opt, snaps = read_format_a(GOLDEN / "output_test.bin")
+    assert len(snaps) == 5
+    for i, s in enumerate(snaps):
+        assert np.all(np.abs(s["t"] - i * opt.ioutInt) <= 1e-9)
+        ph = 3e-6 * opt.gamma * i * opt.ioutInt
+        assert np.all(np.abs(s["S"][:, 0]) <= 1e-9)
+        assert np.all(np.abs(s["S"][:, 1] - math.sin(ph)) <= 1e-9)
+        assert np.all(np.abs(s["S"][:, 2] - math.cos(ph)) <= 1e-9)
+
+
+def test_golden_cases_exercise_the_paths():
+    """The fixture set covers gas collisions, diffuse bounces, failures and
+    edge/corner stops, so bit-exactness above is meaningful."""
+    seen = {"gas": 0, "fail": 0, "bounce": 0}
+    for case in GOLDEN_CASES:
+        _, s = read_format_a(GOLDEN / f"{case}.bin")
+        if len(s) == 0:
+            continue
+        last = s[-1]
+        seen["gas"] += int(last["n_coll"].sum())
+        seen["bounce"] += int(last["n_bounce"].sum())
+        seen["fail"] += int((last["fail"] != 0).sum())
+    assert seen["gas"] > 100 and seen["bounce"] > 1000 and seen["fail"] > 0
