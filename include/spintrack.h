@@ -138,6 +138,16 @@ int st_read_state(st_ctx *ctx, const st_state_view *host);
 /* Borrowed device pointers to the SoA state. */
 int st_device_state(st_ctx *ctx, st_device_soa *out);
 int st_synchronize(st_ctx *ctx);
+/* The context's CUDA stream (cudaStream_t), for callers that order their own
+ * work or time kernels with events on it. */
+void *st_get_stream(st_ctx *ctx);
+/* Replace every set's parameters (same particle counts) without reallocating:
+ * the device parameter table is re-uploaded; call st_init to restart.  Used
+ * for parameter scans.  No counterpart in the reference, which takes options
+ * only at construction (include/particle.h:90). */
+int st_set_params(st_ctx *ctx, const st_options *sets, int nsets);
+/* Bytes of the device parameter table that st_set_params uploads. */
+size_t st_param_table_bytes(const st_ctx *ctx);
 /* Persistent-kernel launch configuration (NULL = autotune on first use). */
 int st_set_launch_config(st_ctx *ctx, const st_launch_config *cfg);
 int st_get_launch_config(const st_ctx *ctx, st_launch_config *cfg);

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -632,6 +633,25 @@ int st_device_state(st_ctx* c, st_device_soa* o) {
   return ST_OK;
 }
 
+void* st_get_stream(st_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int st_set_params(st_ctx* c, const st_options* sets, int nsets) {
+  if (!c || !sets || nsets != (int)c->sets_h.size()) return fail(ST_ERR_ARG, "st_set_params needs one options per set");
+  std::vector<SetParams> P(c->sets_h.size());
+  for (int k = 0; k < nsets; ++k) {
+    if (sets[k].numParticles != c->opts[k].numParticles)
+      return fail(ST_ERR_ARG, "st_set_params cannot change a set's particle count");
+    ST_TRY(build_params(sets[k], c->sets_h[k].first, &P[k]));
+  }
+  ST_CUDA(cudaSetDevice(c->device));
+  ST_CUDA(cudaMemcpyAsync(c->sets_d, P.data(), sizeof(SetParams) * P.size(), cudaMemcpyHostToDevice, c->stream));
+  for (int k = 0; k < nsets; ++k) c->opts[k] = sets[k];
+  c->sets_h = P;
+  return ST_OK;
+}
+
+size_t st_param_table_bytes(const st_ctx* c) { return c ? sizeof(SetParams) * c->sets_h.size() : 0; }
+
 int st_synchronize(st_ctx* c) {
   if (!c) return fail(ST_ERR_ARG, "null context");
   ST_CUDA(cudaStreamSynchronize(c->stream));
@@ -815,31 +835,58 @@ extern "C" int st_main_analysis(const st_options* opt_in, const char* out_path, 
 // ==================================================================== autotune
 namespace {
 
+// Tuned configurations, keyed by the workload's shape, reused by every later
+// context of the process.
+struct TuneKey {
+  int ntypes_mask;  // bit 0: a DOP853 set, bit 1: an RK45 set, bit 2: trajectory-only
+  int log2n;
+  bool operator<(const TuneKey& o) const {
+    return ntypes_mask != o.ntypes_mask ? ntypes_mask < o.ntypes_mask : log2n < o.log2n;
+  }
+};
+std::map<TuneKey, st_launch_config>& tune_cache() {
+  static std::map<TuneKey, st_launch_config> m;
+  return m;
+}
+
 int autotune(st_ctx* c) {
+  TuneKey key{0, 0};
+  for (const auto& P : c->sets_h) key.ntypes_mask |= P.integrator == 0 ? 1 : (P.integrator == 1 ? 2 : 4);
+  while ((int64_t(1) << key.log2n) < c->n) ++key.log2n;
+  auto it = tune_cache().find(key);
+  if (it != tune_cache().end()) {
+    c->lc = it->second;
+    return ST_OK;
+  }
   const int nv = st::persistent_variant_count();
-  // sample: a few particles of every set, one window, on a scratch context
+  // Sample: enough particles to fill two rounds of lanes, every set
+  // represented, one short window (ioutInt capped at 20 ms) on a scratch
+  // context, so each candidate runs for a few milliseconds.
   std::vector<st_options> sample = c->opts;
-  const int64_t lanes_guess = (int64_t)c->sm_count * 256;
-  const int64_t want = std::max<int64_t>(4 * lanes_guess, 1);
+  const int64_t want = std::max<int64_t>((int64_t)c->sm_count * 512, 1);
   const double frac = std::min(1.0, (double)want / (double)std::max<int64_t>(c->n, 1));
   for (auto& o : sample) {
-    o.numParticles = std::max(0, (int)std::ceil(o.numParticles * frac));
-    o.tf = o.t0 + o.ioutInt;  // one window
+    o.numParticles = o.numParticles > 0 ? std::max(1, (int)std::ceil(o.numParticles * frac)) : 0;
+    o.ioutInt = std::min(o.ioutInt, 0.02);
+    o.tf = o.t0 + o.ioutInt;
   }
   st_ctx* s = nullptr;
   ST_TRY(st_create_batch(sample.data(), (int)sample.size(), c->device, &s));
   double best = 1e300;
-  st_launch_config best_cfg{0, 1, 0};
+  st_launch_config best_cfg{0, 1, 1};
   for (int v = 0; v < nv; ++v) {
-    const int maxb = st::persistent_max_blocks_per_sm(v, 0);
-    for (int b = 1; b <= std::max(1, maxb); ++b) {
-      st_launch_config cfg{0, b, v};
+    const int maxb = std::max(1, st::persistent_max_blocks_per_sm(v, 0));
+    const int cands[2] = {1, maxb};
+    for (int k = 0; k < (maxb > 1 ? 2 : 1); ++k) {
+      st_launch_config cfg{0, cands[k], v};
       st_set_launch_config(s, &cfg);
-      if (st_init(s) != ST_OK) break;
-      const double t0 = now_s();
-      const int r = st_run_windows(s, ST_KERNEL_PERSISTENT, 0, 1, nullptr);
-      const double el = now_s() - t0;
-      if (r != ST_OK) continue;
+      double el = 1e300;
+      for (int rep = 0; rep < 2; ++rep) {  // first repetition warms the variant up
+        if (st_init(s) != ST_OK) break;
+        const double t0 = now_s();
+        const int r = st_run_windows(s, ST_KERNEL_PERSISTENT, 0, 1, nullptr);
+        if (r == ST_OK) el = now_s() - t0;
+      }
       if (el < best) {
         best = el;
         best_cfg = cfg;
@@ -848,6 +895,7 @@ int autotune(st_ctx* c) {
   }
   st_destroy(s);
   c->lc = best_cfg;
+  tune_cache()[key] = best_cfg;
   return ST_OK;
 }
 

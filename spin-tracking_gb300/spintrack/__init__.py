@@ -156,6 +156,20 @@ class Particles:
         check(load().st_get_counters(self._ctx, ctypes.byref(c)))
         return {k: int(getattr(c, k)) for k, _ in Counters._fields_}
 
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(load().st_get_stream(self._ctx) or 0)
+
+    def set_params(self, opt: Options | Iterable[Options]) -> None:
+        """Re-upload every set's parameters (same particle counts); call init_particles next."""
+        sets = [opt] if isinstance(opt, Options) else list(opt)
+        arr = (Options * len(sets))(*sets)
+        check(load().st_set_params(self._ctx, arr, len(sets)))
+        self._sets = sets
+
+    def param_table_bytes(self) -> int:
+        return int(load().st_param_table_bytes(self._ctx))
+
     def synchronize(self) -> None:
         check(load().st_synchronize(self._ctx))
 

@@ -89,6 +89,9 @@ _SIGS = {
     "st_read_state": (c_int, [c_void_p, POINTER(StateView)]),
     "st_device_state": (c_int, [c_void_p, POINTER(DeviceSoA)]),
     "st_synchronize": (c_int, [c_void_p]),
+    "st_get_stream": (c_void_p, [c_void_p]),
+    "st_set_params": (c_int, [c_void_p, POINTER(Options), c_int]),
+    "st_param_table_bytes": (c_size_t, [c_void_p]),
     "st_set_launch_config": (c_int, [c_void_p, POINTER(LaunchConfig)]),
     "st_get_launch_config": (c_int, [c_void_p, POINTER(LaunchConfig)]),
     "st_set_deadline": (c_int, [c_void_p, c_double]),
