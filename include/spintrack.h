@@ -162,6 +162,29 @@ typedef struct st_counters {
 } st_counters;
 int st_get_counters(const st_ctx *ctx, st_counters *out);
 
+/* Allocation-free run, for callers that cannot allocate device memory when
+ * they run the tracker (a host whose memory pool owns the GPU, or a hot path
+ * that must not call cudaMalloc/cudaFree because they synchronise the device).
+ * No counterpart in the reference.  Equivalent to st_create_batch + st_init +
+ * st_run_windows(ST_KERNEL_PERSISTENT, 0, w_end) on the current device and
+ * the caller's stream, but every byte it touches is either the caller's
+ * `state` buffer or a 4 KiB scratch array compiled into the library (work
+ * queue cursor, counters, parameter table), held by each GPU that loads the
+ * library until the process exits.  It calls no cudaMalloc/cudaFree.
+ *   state == NULL: writes the required buffer size to *state_bytes, returns.
+ *   state != NULL: a 256-byte aligned device buffer of *state_bytes bytes;
+ *     on return it holds the particle state after window w_end as 27 arrays
+ *     over all particles (sets in order), each starting on a 256-byte
+ *     boundary: t, pos_x, pos_y, pos_z, v_x, v_y, v_z, S_x, S_y, S_z (f64),
+ *     fail (i32), n_coll, n_bounce, n_steps (u64), then internal fields.
+ * At most 8 parameter sets per call (ST_ERR_ARG beyond).  Every call shares
+ * the scratch and it keeps the last call's contents; each call clears what
+ * must start at zero, so calls that overlap on the GPU race and must not be
+ * issued.  The first call on a device looks the scratch address up with
+ * cudaGetSymbolAddress; make it before any stream capture.  Synchronises
+ * `stream` (a cudaStream_t, NULL = default stream) before returning. */
+int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state_bytes, int w_end, void *stream);
+
 /* FP64 FMA issue-rate probe (TFLOP/s, FMA = 2 flops): eight independent
  * DFMA chains per thread on every SM.  No counterpart in the reference; it is
  * the roofline denominator for the step kernels, which are FP64-pipe bound. */

@@ -139,6 +139,12 @@ int build_params(const st_options& o, int64_t first, SetParams* P) {
 
 }  // namespace
 
+// Entry points for other translation units of the library (st_noalloc.cu).
+namespace st {
+int build_set_params(const st_options& o, int64_t first, SetParams* P) { return build_params(o, first, P); }
+int set_last_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace st
+
 // ==================================================================== context
 struct st_ctx {
   int device = 0;

@@ -95,6 +95,9 @@ int launch_until(const RunArgs& a, double next_t, int block, void* stream);
 int launch_arm_deadline(RunStatus* status, unsigned long long budget_ns, void* stream);
 int probe_fp64(int sm_count, int iters, double* seconds, double* flops);
 int persistent_variant_count();
+// Host helpers shared across the library's translation units.
+int build_set_params(const st_options& o, int64_t first, SetParams* P);
+int set_last_error(int code, const char* msg);
 int persistent_max_blocks_per_sm(int variant, int block);
 const char* persistent_variant_name(int variant);
 

@@ -98,6 +98,7 @@ _SIGS = {
     "st_get_counters": (c_int, [c_void_p, POINTER(Counters)]),
     "st_main_analysis": (c_int, [POINTER(Options), c_char_p, c_int, c_int, POINTER(c_double)]),
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),
+    "st_run_noalloc": (c_int, [POINTER(Options), c_int, c_void_p, POINTER(c_size_t), c_int, c_void_p]),
     "st_write_header": (c_int, [c_void_p, POINTER(Options)]),
     "st_write_snapshot": (c_int, [c_void_p, c_int, POINTER(StateView)]),
 }
