@@ -151,6 +151,10 @@ size_t st_param_table_bytes(const st_ctx *ctx);
 /* Persistent-kernel launch configuration (NULL = autotune on first use). */
 int st_set_launch_config(st_ctx *ctx, const st_launch_config *cfg);
 int st_get_launch_config(const st_ctx *ctx, st_launch_config *cfg);
+/* Number of persistent-kernel variants (valid st_launch_config.variant
+ * values are 0 .. count-1) and the name of one, for external tuners. */
+int st_launch_variant_count(void);
+const char *st_launch_variant_name(int variant);
 /* Device time budget for each following run call, in seconds (0 = none).
  * When it runs out, kernels save the particle state and the call returns
  * ST_ERR_DEADLINE; calling again resumes. */
@@ -168,7 +172,7 @@ int st_get_counters(const st_ctx *ctx, st_counters *out);
  * No counterpart in the reference.  Equivalent to st_create_batch + st_init +
  * st_run_windows(ST_KERNEL_PERSISTENT, 0, w_end) on the current device and
  * the caller's stream, but every byte it touches is either the caller's
- * `state` buffer or a 4 KiB scratch array compiled into the library (work
+ * `state` buffer or a 8 KiB scratch array compiled into the library (work
  * queue cursor, counters, parameter table), held by each GPU that loads the
  * library until the process exits.  It calls no cudaMalloc/cudaFree.
  *   state == NULL: writes the required buffer size to *state_bytes, returns.

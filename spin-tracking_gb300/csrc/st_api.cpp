@@ -204,6 +204,8 @@ int ctx_alloc(st_ctx* c) {
   ST_CUDA(cudaMalloc(&c->sets_d, sizeof(SetParams) * std::max<size_t>(c->sets_h.size(), 1)));
   ST_CUDA(cudaMemcpyAsync(c->sets_d, c->sets_h.data(), sizeof(SetParams) * c->sets_h.size(), cudaMemcpyHostToDevice,
                           c->stream));
+  if (int e = st::launch_prepare_sets(c->sets_d, (int)c->sets_h.size(), c->stream))
+    return fail(ST_ERR_CUDA, std::string("prepare sets: ") + cudaGetErrorString((cudaError_t)e));
   ST_CUDA(cudaMalloc(&c->status_d, sizeof(st::RunStatus)));
   ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
   ST_CUDA(cudaMallocHost(&c->status_h, sizeof(st::RunStatus)));
@@ -275,6 +277,7 @@ int end_run(st_ctx* c, int launches) {
   c->last.rk45_attempts = c->status_h->rk45_attempts;
   c->last.segments = c->status_h->segments;
   c->last.kernel_launches = (uint64_t)launches;
+  if (c->status_h->pad) return fail(ST_ERR_CUDA, "internal: a persistent-kernel lane could not make progress");
   if (c->status_h->deadline_hit) return fail(ST_ERR_DEADLINE, "device time budget ran out; state saved at window ends");
   return ST_OK;
 }
@@ -651,6 +654,8 @@ int st_set_params(st_ctx* c, const st_options* sets, int nsets) {
   }
   ST_CUDA(cudaSetDevice(c->device));
   ST_CUDA(cudaMemcpyAsync(c->sets_d, P.data(), sizeof(SetParams) * P.size(), cudaMemcpyHostToDevice, c->stream));
+  if (int e = st::launch_prepare_sets(c->sets_d, nsets, c->stream))
+    return fail(ST_ERR_CUDA, std::string("prepare sets: ") + cudaGetErrorString((cudaError_t)e));
   for (int k = 0; k < nsets; ++k) c->opts[k] = sets[k];
   c->sets_h = P;
   return ST_OK;
@@ -677,6 +682,9 @@ int st_set_launch_config(st_ctx* c, const st_launch_config* cfg) {
   }
   return ST_OK;
 }
+
+int st_launch_variant_count(void) { return st::persistent_variant_count(); }
+const char* st_launch_variant_name(int v) { return st::persistent_variant_name(v); }
 
 int st_get_launch_config(const st_ctx* c, st_launch_config* cfg) {
   if (!c || !cfg) return fail(ST_ERR_ARG, "null argument");

@@ -431,44 +431,67 @@ struct Seg {
   bool reject, last;
 };
 
-__device__ __forceinline__ void seg_setup(Seg& g, const SetParams& P, const SegStart& s0, double t_end) {
+// The per-set field constants (launch_prepare_sets): gamma * B0, the gradient
+// tensor's columns through the st_grad hook, gamma * E / c^2 and the gravity
+// terms of the segment polynomial.
+__device__ inline void prepare_set(SetParams& P) {
   const double gm = P.gamma;
-  const Vec3 p0 = {s0.px, s0.py, s0.pz};
-  const Vec3 v0 = {s0.vx, s0.vy, s0.vz};
-  const double cx = s0.vy * P.Ez - s0.vz * P.Ey;
-  const double cy = s0.vz * P.Ex - s0.vx * P.Ez;
-  const double cz = s0.vx * P.Ey - s0.vy * P.Ex;
   const double g_ = P.gravity ? kGravity : 0.0;
+  P.gB0[0] = gm * P.B0x; P.gB0[1] = gm * P.B0y; P.gB0[2] = gm * P.B0z;
+  const Vec3 ex = {1.0, 0.0, 0.0}, ey = {0.0, 1.0, 0.0}, ez = {0.0, 0.0, 1.0};
+  const Vec3 c0 = st_grad(ex, P), c1 = st_grad(ey, P), c2 = st_grad(ez, P);
+  P.gGc[0][0] = gm * c0.x; P.gGc[0][1] = gm * c0.y; P.gGc[0][2] = gm * c0.z;
+  P.gGc[1][0] = gm * c1.x; P.gGc[1][1] = gm * c1.y; P.gGc[1][2] = gm * c1.z;
+  P.gGc[2][0] = gm * c2.x; P.gGc[2][1] = gm * c2.y; P.gGc[2][2] = gm * c2.z;
+  P.gEc[0] = gm * P.inv_c2 * P.Ex; P.gEc[1] = gm * P.inv_c2 * P.Ey; P.gEc[2] = gm * P.inv_c2 * P.Ez;
+  // d/dtau of v x E along the parabola: (g yhat) x E = g (Ez, 0, -Ex)
+  P.o1g[0] = gm * P.inv_c2 * g_ * P.Ez; P.o1g[1] = 0.0; P.o1g[2] = -gm * P.inv_c2 * g_ * P.Ex;
 #if ST_GRAD_IS_LINEAR
-  const Vec3 Gp = st_grad(p0, P);
-  const Vec3 Gv = st_grad(v0, P);
-  const Vec3 Gy = st_grad(Vec3{0.0, 1.0, 0.0}, P);
-  g.o0x = gm * (P.B0x + Gp.x + P.inv_c2 * cx);
-  g.o0y = gm * (P.B0y + Gp.y + P.inv_c2 * cy);
-  g.o0z = gm * (P.B0z + Gp.z + P.inv_c2 * cz);
-  // d/dtau: grad(v0) and the gravity term of v x E, (g yhat) x E = g (Ez, 0, -Ex)
-  g.o1x = gm * (Gv.x + P.inv_c2 * g_ * P.Ez);
-  g.o1y = gm * (Gv.y);
-  g.o1z = gm * (Gv.z - P.inv_c2 * g_ * P.Ex);
-  g.o2x = gm * (0.5 * g_ * Gy.x);
-  g.o2y = gm * (0.5 * g_ * Gy.y);
-  g.o2z = gm * (0.5 * g_ * Gy.z);
+  P.o2c[0] = 0.5 * g_ * P.gGc[1][0]; P.o2c[1] = 0.5 * g_ * P.gGc[1][1]; P.o2c[2] = 0.5 * g_ * P.gGc[1][2];
 #else
-  g.p0x = p0.x; g.p0y = p0.y; g.p0z = p0.z;
-  g.v0x = v0.x; g.v0y = v0.y; g.v0z = v0.z;
-  g.o0x = gm * (P.B0x + P.inv_c2 * cx);
-  g.o0y = gm * (P.B0y + P.inv_c2 * cy);
-  g.o0z = gm * (P.B0z + P.inv_c2 * cz);
-  g.o1x = gm * (P.inv_c2 * g_ * P.Ez);
-  g.o1y = 0.0;
-  g.o1z = gm * (-P.inv_c2 * g_ * P.Ex);
-  g.o2x = g.o2y = g.o2z = 0.0;
+  P.o2c[0] = P.o2c[1] = P.o2c[2] = 0.0;  // the hook is evaluated at every stage instead
 #endif
-  g.gpa = gm * P.a;
-  g.t0 = s0.t;
+}
+
+// Coefficients o0, o1 of the field polynomial of a segment starting at (p0, v0).
+__device__ __forceinline__ void seg_field(const SetParams& P, double px, double py, double pz, double vx, double vy,
+                                          double vz, double o0[3], double o1[3]) {
+  const double* e = P.gEc;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    // v0 x gEc, component c
+    const double cr = (c == 0) ? fma(vy, e[2], -vz * e[1]) : (c == 1) ? fma(vz, e[0], -vx * e[2]) : fma(vx, e[1], -vy * e[0]);
+#if ST_GRAD_IS_LINEAR
+    o0[c] = P.gB0[c] + fma(px, P.gGc[0][c], fma(py, P.gGc[1][c], fma(pz, P.gGc[2][c], cr)));
+    o1[c] = fma(vx, P.gGc[0][c], fma(vy, P.gGc[1][c], fma(vz, P.gGc[2][c], P.o1g[c])));
+#else
+    o0[c] = P.gB0[c] + cr;
+    o1[c] = P.o1g[c];
+#endif
+  }
+}
+
+// Fill the integrator's segment from its field coefficients and time span.
+__device__ __forceinline__ void seg_begin(Seg& g, const SetParams& P, double t0, double t_end, const double o0[3],
+                                          const double o1[3]) {
+  g.o0x = o0[0]; g.o0y = o0[1]; g.o0z = o0[2];
+  g.o1x = o1[0]; g.o1y = o1[1]; g.o1z = o1[2];
+  g.o2x = P.o2c[0]; g.o2y = P.o2c[1]; g.o2z = P.o2c[2];
+  g.gpa = P.gamma * P.a;
+  g.t0 = t0;
   g.xf = t_end;
-  g.x = s0.t;
-  g.posneg = (t_end - s0.t < 0.0) ? -1.0 : 1.0;
+  g.x = t0;
+  g.posneg = (t_end - t0 < 0.0) ? -1.0 : 1.0;
+}
+
+__device__ __forceinline__ void seg_setup(Seg& g, const SetParams& P, const SegStart& s0, double t_end) {
+  double o0[3], o1[3];
+  seg_field(P, s0.px, s0.py, s0.pz, s0.vx, s0.vy, s0.vz, o0, o1);
+  seg_begin(g, P, s0.t, t_end, o0, o1);
+#if !ST_GRAD_IS_LINEAR
+  g.p0x = s0.px; g.p0y = s0.py; g.p0z = s0.pz;
+  g.v0x = s0.vx; g.v0y = s0.vy; g.v0z = s0.vz;
+#endif
 }
 
 // Omega = gamma * B at tau = t - t0.

@@ -24,6 +24,15 @@ struct SetParams {
   double Gx[3], Gy[3], Gz[3];     // rows: B_i = dot(pos, G_i)
   double a, w;                    // pulse amplitude and angular frequency
   double inv_c2;                  // 1.0 / c^2 as the reference evaluates it
+  // Field constants of the segment polynomial, filled on the device from the
+  // st_grad hook by launch_prepare_sets:
+  //   Omega(tau) = o0 + tau (o1 + tau o2),
+  //   o0 = gB0 + sum_j p0_j gGc[j] + v0 x gEc,  o1 = sum_j v0_j gGc[j] + o1g,  o2 = o2c.
+  double gB0[3];                  // gamma * B0
+  double gGc[3][3];               // gamma * grad(e_j): column j of the gradient tensor
+  double gEc[3];                  // gamma * E / c^2
+  double o1g[3];                  // gamma * (g yhat x E) / c^2 (gravity)
+  double o2c[3];                  // gamma * (g / 2) * grad(yhat) (gravity)
   // ---- stepper (src/integrator.cpp:90-337)
   double rtol, atol, hmin, hmax, h0, safe, fac1, fac2, beta;
   double facc1, facc2, expo1, inv_safe;
@@ -69,7 +78,7 @@ struct RunStatus {
   unsigned long long queue_head;   // persistent-kernel work queue cursor
   unsigned long long deadline_ns;  // %globaltimer value after which lanes stop (0 = none)
   int deadline_hit;
-  int pad;
+  int pad;                         // set by a kernel that detected an internal logic error
 };
 
 struct RunArgs {
@@ -87,6 +96,7 @@ struct RunArgs {
 
 // Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
 // cast to int (0 = success).
+int launch_prepare_sets(SetParams* sets, int nsets, void* stream);
 int launch_init(const RunArgs& a, int block, void* stream);
 int launch_plain_window(const RunArgs& a, int window, int block, void* stream);
 int launch_pack_snapshot(const RunArgs& a, int slot, void* stream);

@@ -69,6 +69,12 @@ __device__ __forceinline__ void write_snap(const RunArgs& a, int64_t i, int w, c
   reinterpret_cast<uint64_t*>(b + o[13])[i] = p.n_steps;
 }
 
+// ------------------------------------------------------------------ set constants
+__global__ void k_prepare_sets(SetParams* sets, int nsets) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nsets) prepare_set(sets[k]);
+}
+
 // ------------------------------------------------------------------ init
 __global__ void k_init(RunArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,6 +306,231 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent(RunArgs a) {
   }
 }
 
+// ------------------------------------------------------------------ batched (trajectory ahead)
+// The trajectory of a particle does not depend on its spin, so each lane runs
+// its particle's trajectory ahead of the spin integration into a small ring of
+// segment records in shared memory.  Rings are topped up warp-synchronously,
+// only when many lanes have room (or one lane has run dry), so the long and
+// branchy trajectory code runs with most lanes of the warp active instead of
+// the few lanes whose segment just ended.  A record carries the segment's time
+// span and field polynomial (o0, o1), so starting a segment on the spin side
+// is a ring pop and one Bloch evaluation.  The trajectory stops at every
+// window end until the spin side has finished the window, so checkpoints and
+// snapshots at window ends are exact.
+//
+// Record fields (field-major, conflict-free): qd[(slot * kRecF + f) * BLOCK + tid]
+//   f = 0 t_start, 1 t_end, 2..4 o0, 5..7 o1 (+ 8..13 p0, v0 when the grad hook is not linear)
+// flags qf[slot * BLOCK + tid]: bit0 window end reached, bit1 stop, bit2 bounce, bit3 gas
+// collision, bits 8-15 sanity failure code.
+constexpr int kRecF = ST_GRAD_IS_LINEAR ? 8 : 14;
+
+template <int BLOCK>
+__device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, double tf, double* qd, int* qf,
+                                               int slot, int tid, bool& blocked) {
+  SegStart s0;
+  const uint64_t nb = tp.n_bounce, nc = tp.n_coll;
+  const bool fin = traj_event(tp, P, tf, s0);
+  double* r = qd + (size_t)slot * kRecF * BLOCK + tid;
+  r[0 * BLOCK] = s0.t;
+  r[1 * BLOCK] = tp.t;
+  if (P.integrator == 0 || P.integrator == 1) {
+    double o0[3], o1[3];
+    seg_field(P, s0.px, s0.py, s0.pz, s0.vx, s0.vy, s0.vz, o0, o1);
+    r[2 * BLOCK] = o0[0]; r[3 * BLOCK] = o0[1]; r[4 * BLOCK] = o0[2];
+    r[5 * BLOCK] = o1[0]; r[6 * BLOCK] = o1[1]; r[7 * BLOCK] = o1[2];
+#if !ST_GRAD_IS_LINEAR
+    r[8 * BLOCK] = s0.px; r[9 * BLOCK] = s0.py; r[10 * BLOCK] = s0.pz;
+    r[11 * BLOCK] = s0.vx; r[12 * BLOCK] = s0.vy; r[13 * BLOCK] = s0.vz;
+#endif
+  }
+  qf[slot * BLOCK + tid] = (fin ? 1 : 0) | (tp.stop ? 2 : 0) | (tp.n_bounce != nb ? 4 : 0) |
+                           (tp.n_coll != nc ? 8 : 0) | ((tp.fail & 0xff) << 8);
+  if (fin || tp.stop) blocked = true;
+}
+
+enum BatchedMode { B_FETCH = 0, B_NEED = 1, B_SEG = 2, B_WEND = 3, B_DONE = 4 };
+
+template <int BLOCK, int MINB, int QCAP>
+__global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_start, int topup_keep) {
+  extern __shared__ double st_smem[];
+  double* qd = st_smem;
+  int* qf = reinterpret_cast<int*>(st_smem + (size_t)QCAP * kRecF * BLOCK);
+  const int tid = threadIdx.x;
+  const unsigned FULL = 0xffffffffu;
+  int mode = B_FETCH;
+  int64_t i = 0;
+  const SetParams* P = a.sets;
+  PState tp;  // trajectory fields run ahead; S, h, n_steps belong to the spin side
+  Seg g;
+  uint64_t s_ncoll = 0, s_nbounce = 0;
+  int s_fail = 0;
+  bool s_stop = false, cur_fin = false, blocked = true;
+  int w = 0, wlast = 0, qhead = 0, qcount = 0;
+  double tf = 0.0, tempH = 0.0;
+  unsigned long long n_dop = 0, n_rk = 0, n_seg = 0;
+  unsigned int tick = 0, dry = 0;
+  bool hit = false;
+  const unsigned long long dl = run_deadline(a);
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  while (true) {
+    // ---- A: spin-side boundaries of this lane (pop records, window ends, fetch)
+    bool starved = false;
+#pragma unroll 1
+    for (int guard = 0; guard < 8; ++guard) {
+      if (mode == B_FETCH) {
+        const unsigned long long item = atomicAdd(&a.status->queue_head, 1ull);
+        if (item >= (unsigned long long)a.s.n) {
+          mode = B_DONE;
+          break;
+        }
+        i = a.order ? a.order[item] : (int64_t)item;
+        P = &a.sets[a.s.set[i]];
+        w = a.s.w_done[i];
+        wlast = min(a.w_end, P->nwin);
+        if (w >= wlast) continue;
+        tp = load_state(a.s, i);
+        s_fail = tp.fail;
+        s_stop = tp.stop;
+        s_ncoll = tp.n_coll;
+        s_nbounce = tp.n_bounce;
+        qhead = qcount = 0;
+        tf = ((double)w + 1.0) * P->ioutInt;
+        tempH = tp.h;
+        blocked = s_stop;
+        mode = s_stop ? B_WEND : B_NEED;
+      } else if (mode == B_NEED) {
+        if (qcount == 0) {
+          starved = true;
+          break;
+        }
+        const int slot = qhead;
+        qhead = (qhead + 1 == QCAP) ? 0 : qhead + 1;
+        --qcount;
+        const double* r = qd + (size_t)slot * kRecF * BLOCK + tid;
+        const int flags = qf[slot * BLOCK + tid];
+        if (flags & 4) ++s_nbounce;
+        if (flags & 8) ++s_ncoll;
+        cur_fin = (flags & 1) != 0;
+        const int code = (int)(signed char)((flags >> 8) & 0xff);
+        if (code != 0) {
+          s_fail = code;
+          s_stop = true;
+        } else if (flags & 2) {
+          s_stop = true;  // diffuse hit on an edge or corner
+        }
+        if (s_stop) {
+          tp.Sx = tp.Sy = tp.Sz = nan;
+          tp.n_steps += 1;
+          mode = B_WEND;
+        } else if (P->integrator == 0 || P->integrator == 1) {
+          const double o0[3] = {r[2 * BLOCK], r[3 * BLOCK], r[4 * BLOCK]};
+          const double o1[3] = {r[5 * BLOCK], r[6 * BLOCK], r[7 * BLOCK]};
+          seg_begin(g, *P, r[0], r[1 * BLOCK], o0, o1);
+#if !ST_GRAD_IS_LINEAR
+          g.p0x = r[8 * BLOCK]; g.p0y = r[9 * BLOCK]; g.p0z = r[10 * BLOCK];
+          g.v0x = r[11 * BLOCK]; g.v0y = r[12 * BLOCK]; g.v0z = r[13 * BLOCK];
+#endif
+          if (P->integrator == 0)
+            dop_begin(g, *P, tp.Sx, tp.Sy, tp.Sz, tempH);
+          else
+            rk45_begin(g, tempH);
+          mode = B_SEG;
+          break;
+        } else {  // trajectory only: the segment completes at once
+          tp.n_steps += 1;
+          if (cur_fin) mode = B_WEND;
+        }
+      } else if (mode == B_WEND) {
+        PState out = tp;
+        out.n_coll = s_ncoll;
+        out.n_bounce = s_nbounce;
+        out.fail = s_fail;
+        out.stop = s_stop;
+        if (s_stop) nan_fill(out);
+        write_snap(a, i, w, out);
+        ++w;
+        store_state(a.s, i, out);  // every window end is a resumable checkpoint
+        a.s.w_done[i] = w;
+        if (w < wlast) {
+          tf = ((double)w + 1.0) * P->ioutInt;
+          tempH = tp.h;
+          blocked = s_stop;
+          mode = s_stop ? B_WEND : B_NEED;
+        } else {
+          mode = B_FETCH;
+        }
+      } else {
+        break;  // B_SEG or B_DONE
+      }
+    }
+    // ---- B: warp-synchronous trajectory top-up
+    const unsigned starved_m = __ballot_sync(FULL, starved);
+    bool prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP;
+    unsigned pm = __ballot_sync(FULL, prod);
+    if (starved_m != 0u || __popc(pm) >= topup_start) {
+#pragma unroll 1
+      for (int round = 0; round < QCAP; ++round) {
+        if (prod) {
+          int slot = qhead + qcount;
+          if (slot >= QCAP) slot -= QCAP;
+          produce_record<BLOCK>(tp, *P, tf, qd, qf, slot, tid, blocked);
+          ++qcount;
+          ++n_seg;
+        }
+        prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP;
+        pm = __ballot_sync(FULL, prod);
+        if (pm == 0u || __popc(pm) < topup_keep) break;
+      }
+      if (starved_m != 0u) {
+        // a starved lane always gets a record in round 0; this bound only
+        // protects the device from a logic error
+        if (++dry > 1000000u) {
+          hit = true;
+          atomicExch(&a.status->pad, 1);
+          break;
+        }
+        continue;
+      }
+    }
+    dry = 0;
+    if (__all_sync(FULL, mode == B_DONE)) break;
+    // ---- C: one step attempt for every lane with an open segment
+    if (mode == B_SEG) {
+      int r;
+      if (P->integrator == 0) {
+        r = dop_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
+        ++n_dop;
+      } else {
+        r = rk45_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
+        ++n_rk;
+      }
+      if (r != 0) {
+        tempH = g.h;
+        if (P->keep) tp.h = tempH;
+        if (r < 0) {
+          s_fail = r;
+          s_stop = true;
+          qcount = 0;  // records computed past the failure are dropped
+          blocked = true;
+        }
+        if (s_stop) tp.Sx = tp.Sy = tp.Sz = nan;
+        tp.n_steps += 1;
+        mode = (cur_fin || s_stop) ? B_WEND : B_NEED;
+      }
+    }
+    if (((++tick) & 255u) == 0u && __any_sync(FULL, past_deadline(dl))) {
+      hit = true;
+      break;
+    }
+  }
+  if (hit) atomicExch(&a.status->deadline_hit, 1);
+  if (a.count_work) {
+    warp_add(&a.status->dop_attempts, n_dop);
+    warp_add(&a.status->rk45_attempts, n_rk);
+    warp_add(&a.status->segments, n_seg);
+  }
+}
+
 // ------------------------------------------------------------------ FP64 peak probe
 // Eight independent DFMA chains per thread: the FP64 pipe's issue rate, the
 // denominator of the step kernels' roofline.
@@ -339,6 +570,12 @@ int probe_fp64(int sm_count, int iters, double* seconds, double* flops) {
 
 // ------------------------------------------------------------------ launchers
 static inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+
+int launch_prepare_sets(SetParams* sets, int nsets, void* stream) {
+  if (nsets <= 0) return 0;
+  k_prepare_sets<<<(nsets + 127) / 128, 128, 0, (cudaStream_t)stream>>>(sets, nsets);
+  return (int)cudaGetLastError();
+}
 
 int launch_init(const RunArgs& a, int block, void* stream) {
   if (a.s.n == 0) return 0;
@@ -380,39 +617,64 @@ int launch_pack_snapshot(const RunArgs& a, int slot, void* stream) {
   return (int)cudaGetLastError();
 }
 
-// Persistent-kernel variants: (block threads, min resident blocks per SM).
-// The second number sets the register budget the compiler may use.
+// Persistent-kernel variants.  Family 0: the flattened kernel (k_persistent);
+// family 1: the trajectory-ahead kernel (k_batched) with its ring capacity
+// and top-up thresholds (start when this many lanes have room, keep filling
+// while this many still have room).  Block threads and the minimum resident
+// blocks per SM set the register budget.
 struct Variant {
-  int block, minb;
+  int family, block, minb, qcap, tstart, tkeep;
   const char* name;
 };
 static const Variant kVariants[] = {
-    {128, 1, "b128_m1"}, {128, 2, "b128_m2"}, {128, 3, "b128_m3"}, {64, 4, "b64_m4"}, {256, 1, "b256_m1"},
+    {0, 128, 1, 0, 0, 0, "flat_b128_m1"},  {0, 128, 2, 0, 0, 0, "flat_b128_m2"},
+    {0, 128, 3, 0, 0, 0, "flat_b128_m3"},  {0, 64, 4, 0, 0, 0, "flat_b64_m4"},
+    {0, 256, 1, 0, 0, 0, "flat_b256_m1"},  {1, 128, 1, 6, 24, 16, "ahead_b128_q6_t24"},
+    {1, 128, 1, 6, 16, 12, "ahead_b128_q6_t16"}, {1, 128, 2, 4, 24, 16, "ahead_b128_q4_t24"},
+    {1, 64, 2, 8, 24, 16, "ahead_b64_q8_t24"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int persistent_variant_count() { return kNumVariants; }
 const char* persistent_variant_name(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "?"; }
 
-template <int B, int M>
-static const void* persistent_fn() {
-  return reinterpret_cast<const void*>(&k_persistent<B, M>);
-}
 static const void* variant_fn(int v) {
   switch (v) {
-    case 0: return persistent_fn<128, 1>();
-    case 1: return persistent_fn<128, 2>();
-    case 2: return persistent_fn<128, 3>();
-    case 3: return persistent_fn<64, 4>();
-    default: return persistent_fn<256, 1>();
+    case 0: return reinterpret_cast<const void*>(&k_persistent<128, 1>);
+    case 1: return reinterpret_cast<const void*>(&k_persistent<128, 2>);
+    case 2: return reinterpret_cast<const void*>(&k_persistent<128, 3>);
+    case 3: return reinterpret_cast<const void*>(&k_persistent<64, 4>);
+    case 4: return reinterpret_cast<const void*>(&k_persistent<256, 1>);
+    case 5:
+    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6>);
+    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4>);
+    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8>);
   }
+}
+
+static size_t variant_smem(int v) {
+  const Variant& x = kVariants[v];
+  if (x.family == 0) return 0;
+  return (size_t)x.qcap * x.block * (kRecF * sizeof(double) + sizeof(int));
+}
+
+// Opt the kernels that need more than 48 KiB of dynamic shared memory in, once.
+static cudaError_t ensure_smem(int v) {
+  static bool done[kNumVariants] = {};
+  if (done[v]) return cudaSuccess;
+  const size_t sm = variant_smem(v);
+  cudaError_t e = cudaSuccess;
+  if (sm > 0) e = cudaFuncSetAttribute(variant_fn(v), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess) done[v] = true;
+  return e;
 }
 
 int persistent_max_blocks_per_sm(int v, int block) {
   int nb = 0;
   if (v < 0 || v >= kNumVariants) return 0;
-  if (block <= 0) block = kVariants[v].block;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, variant_fn(v), block, 0);
+  (void)block;
+  if (ensure_smem(v) != cudaSuccess) return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, variant_fn(v), kVariants[v].block, variant_smem(v));
   return nb;
 }
 
@@ -420,10 +682,15 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
   if (a.s.n == 0) return 0;
   if (v < 0 || v >= kNumVariants) return (int)cudaErrorInvalidValue;
   (void)block;
-  const int b = kVariants[v].block;
+  const Variant& x = kVariants[v];
+  cudaError_t e = ensure_smem(v);
+  if (e != cudaSuccess) return (int)e;
   RunArgs args = a;
-  void* params[] = {&args};
-  cudaError_t e = cudaLaunchKernel(variant_fn(v), dim3(blocks), dim3(b), params, 0, (cudaStream_t)stream);
+  int t0 = x.tstart, t1 = x.tkeep;
+  void* params_flat[] = {&args};
+  void* params_ahead[] = {&args, &t0, &t1};
+  e = cudaLaunchKernel(variant_fn(v), dim3(blocks), dim3(x.block), x.family == 0 ? params_flat : params_ahead,
+                       variant_smem(v), (cudaStream_t)stream);
   return (int)e;
 }
 

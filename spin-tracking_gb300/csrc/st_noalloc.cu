@@ -13,7 +13,7 @@
 //
 // Limits and rules:
 //  * at most kNoAllocMaxSets parameter sets per call (the scratch is
-//    kNoAllocScratchBytes = 4 KiB); more are rejected with ST_ERR_ARG;
+//    kNoAllocScratchBytes = 8 KiB); more are rejected with ST_ERR_ARG;
 //  * all calls on a device share the one scratch array and it keeps the last
 //    call's contents; every call clears the parts that must start at zero
 //    before launching, so calls that overlap on the GPU (different streams or
@@ -33,7 +33,7 @@
 namespace st {
 
 constexpr int kNoAllocMaxSets = 8;
-constexpr size_t kNoAllocScratchBytes = 4096;
+constexpr size_t kNoAllocScratchBytes = 8192;
 constexpr size_t kNoAllocStatusBytes = 256;  // RunStatus, padded
 static_assert(sizeof(RunStatus) <= kNoAllocStatusBytes, "status block");
 static_assert(kNoAllocStatusBytes + kNoAllocMaxSets * sizeof(SetParams) <= kNoAllocScratchBytes, "scratch size");
@@ -124,7 +124,7 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
   using namespace st;
   if (!sets || !state_bytes_io) return set_last_error(ST_ERR_ARG, "st_run_noalloc: null argument");
   if (nsets < 1 || nsets > kNoAllocMaxSets)
-    return set_last_error(ST_ERR_ARG, "st_run_noalloc: 1 to 8 parameter sets per call (4 KiB device scratch)");
+    return set_last_error(ST_ERR_ARG, "st_run_noalloc: 1 to 8 parameter sets per call (8 KiB device scratch)");
   SetParams table[kNoAllocMaxSets];
   int64_t n = 0;
   for (int k = 0; k < nsets; ++k) {
@@ -167,6 +167,7 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
   a.w_end = w_end;
   a.deadline_armed = 0;
   a.count_work = 1;
+  if (int pe = launch_prepare_sets(params, nsets, st_)) return set_last_error(ST_ERR_CUDA, cudaGetErrorString((cudaError_t)pe));
   if (n > 0) {
     k_noalloc_sets<<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(a.s, params, nsets);
     e = cudaGetLastError();

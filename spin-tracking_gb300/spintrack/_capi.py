@@ -95,6 +95,8 @@ _SIGS = {
     "st_set_launch_config": (c_int, [c_void_p, POINTER(LaunchConfig)]),
     "st_get_launch_config": (c_int, [c_void_p, POINTER(LaunchConfig)]),
     "st_set_deadline": (c_int, [c_void_p, c_double]),
+    "st_launch_variant_count": (c_int, []),
+    "st_launch_variant_name": (c_char_p, [c_int]),
     "st_get_counters": (c_int, [c_void_p, POINTER(Counters)]),
     "st_main_analysis": (c_int, [POINTER(Options), c_char_p, c_int, c_int, POINTER(c_double)]),
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),

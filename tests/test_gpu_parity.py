@@ -87,3 +87,25 @@ def test_run_until_matches_window_driver(gpu):
         a, b = p.output_data(), q.output_data()
     for f in a:
         np.testing.assert_array_equal(a[f], b[f], err_msg=f)
+
+
+@pytest.mark.parametrize("case", ["m04_gas", "c_gas", "m42_diffuse", "nmax", "rk45", "traj", "pulse"])
+def test_every_persistent_variant_matches_plain(gpu, case):
+    """Every launch variant of the batched engine (the flattened kernel and the
+    trajectory-ahead kernel with each ring size and top-up rule) runs the same
+    device arithmetic as the plain kernel: outputs must be identical."""
+    from spintrack import _capi
+    opt = st.derive(st.parse_params(GOLDEN / f"{case}.params"))
+    nwin = st.num_windows(opt)
+    with st.Particles(opt) as p:
+        p.init_particles()
+        p.run_windows(0, nwin, st.KERNEL_PLAIN)
+        ref = p.output_data()
+    for v in range(_capi.load().st_launch_variant_count()):
+        with st.Particles(opt) as p:
+            p.set_launch_config(v, 0)
+            p.init_particles()
+            p.run_windows(0, nwin, st.KERNEL_PERSISTENT)
+            got = p.output_data()
+        for f in ref:
+            np.testing.assert_array_equal(got[f], ref[f], err_msg=f"variant {v} field {f}")
