@@ -135,6 +135,9 @@ size_t st_snapshot_field_offset(const st_ctx *ctx, int field);
 /* particle::outputData, src/particle.cpp:852-862: synchronise and copy the
  * eight snapshot fields of every particle to host arrays. */
 int st_read_state(st_ctx *ctx, const st_state_view *host);
+/* Copy every particle's spin into a dense device array (3 doubles per
+ * particle, set order) and wait for the copy. */
+int st_gather_spins(st_ctx *ctx, double *dst_device);
 /* Borrowed device pointers to the SoA state. */
 int st_device_state(st_ctx *ctx, st_device_soa *out);
 int st_synchronize(st_ctx *ctx);
@@ -188,6 +191,26 @@ int st_get_counters(const st_ctx *ctx, st_counters *out);
  * cudaGetSymbolAddress; make it before any stream capture.  Synchronises
  * `stream` (a cudaStream_t, NULL = default stream) before returning. */
 int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state_bytes, int w_end, void *stream);
+
+/* ---- discrete adjoint (DOP853, fixed accepted-step sequence) ----------- */
+/* Gradient parameters, in this order: the gradient tensor rows Gx, Gy, Gz
+ * (9: B_i = dot(pos, G_i)), B0 (3), E (3), pulse amplitude a and angular
+ * frequency w (2). */
+#define ST_NUM_THETA 17
+/* Forward pass for st_adjoint_backward, from a freshly initialised context
+ * (st_init): advances every particle through windows [0, w_end) exactly as
+ * st_run_windows does, and stores a full-state checkpoint every
+ * segments_per_checkpoint trajectory segments (0 = 64) in a device pool of
+ * pool_bytes (0 = a quarter of free device memory).  ST_ERR_NOMEM if the pool
+ * runs out.  DOP853 sets only.  No counterpart in the reference (it has no
+ * derivatives); the forward arithmetic is the engine's own. */
+int st_adjoint_record(st_ctx *ctx, int w_end, int segments_per_checkpoint, size_t pool_bytes);
+/* Backward pass: given dL/dS_final for every particle (device array,
+ * 3 doubles per particle, set order), writes dL/dtheta per particle (device
+ * array, ST_NUM_THETA doubles per particle); sum over a set's particles for
+ * the set's gradient.  Particles that stopped (failure codes) get zeros.
+ * flags bit 0: also differentiate the pulse (a, w), one sincos per stage. */
+int st_adjoint_backward(st_ctx *ctx, const double *dL_dS, double *grad, int flags);
 
 /* FP64 FMA issue-rate probe (TFLOP/s, FMA = 2 flops): eight independent
  * DFMA chains per thread on every SM.  No counterpart in the reference; it is

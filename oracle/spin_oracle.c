@@ -32,6 +32,21 @@ static const double OR_C2 = 299792458.0 * 299792458.0;
 static or_counters *g_counters = NULL;
 void or_set_counters(or_counters *c) { g_counters = c; }
 
+/* Frozen accepted-step log (finite-difference checks of the adjoint): mode 1
+ * appends every accepted DOP853 step (h, last) to the log; mode 2 replays the
+ * log instead of the step controller (every step accepted with the logged h).
+ * Runs that use the log must be single-threaded. */
+static double *g_log = NULL;
+static int64_t g_log_cap = 0, g_log_n = 0;
+static int g_log_mode = 0;
+void or_set_step_log(double *buf, int64_t cap, int mode) {
+  g_log = buf;
+  g_log_cap = cap;
+  g_log_n = 0;
+  g_log_mode = mode;
+}
+int64_t or_step_log_count(void) { return g_log_n; }
+
 /* ---------------------------------------------------------------- vec3 ops
  * Component-wise restatements of the reference `coords` operators
  * (src/double3.cpp:21-145).  Each returns a new value; order is preserved. */
@@ -402,11 +417,21 @@ int or_integrate_dop(const or_options *o, double t0, double tf, or_vec3 *yio, co
       *hio = h;
       return -1;
     }
-    if ((x + 1.01 * h - xf) * posneg > 0.0) {
-      h = xf - x;
-      last = 1;
+    if (g_log_mode == 2) { /* replay: the logged accepted step */
+      if (g_log_n >= g_log_cap) {
+        *yio = y;
+        return -9;
+      }
+      h = g_log[2 * g_log_n];
+      last = g_log[2 * g_log_n + 1] != 0.0;
+      g_log_n++;
+    } else {
+      if ((x + 1.01 * h - xf) * posneg > 0.0) {
+        h = xf - x;
+        last = 1;
+      }
+      if (h < o->hmin && last != 1) h = o->hmin;
     }
-    if (h < o->hmin && last != 1) h = o->hmin;
     nstep++;
     if (g_counters) {
 #pragma omp atomic
@@ -440,7 +465,12 @@ int or_integrate_dop(const or_options *o, double t0, double tf, or_vec3 *yio, co
     double fac = fac11 / pow(facold, o->beta);
     fac = dmax(facc2, dmin(facc1, fac / o->safe));
     double hnew = h / fac;
-    if (err <= 1.0 || o->fixedStepSize) {
+    if (err <= 1.0 || o->fixedStepSize || g_log_mode == 2) {
+      if (g_log_mode == 1 && g_log_n < g_log_cap) {
+        g_log[2 * g_log_n] = h;
+        g_log[2 * g_log_n + 1] = last ? 1.0 : 0.0;
+        g_log_n++;
+      }
       facold = dmax(err, 1.0e-4);
       naccpt++;
       k[1] = bloch(o, xph, k5, t0, p_old, v_old);

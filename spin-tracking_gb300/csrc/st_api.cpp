@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "spintrack.h"
+#include "st_fields.cuh"
 #include "st_internal.h"
 
 using st::SetParams;
@@ -165,6 +166,21 @@ struct st_ctx {
   double deadline_s = 0.0;
   st_counters last{};
   st::SnapLayout snap{};
+  bool fresh = false;        // st_init ran and no run call since
+  // adjoint (allocated by st_adjoint_record)
+  void* adj_pool = nullptr;
+  int64_t adj_pool_cap = 0;
+  unsigned long long* adj_head = nullptr;
+  int* adj_overflow = nullptr;
+  int64_t* adj_last = nullptr;
+  int64_t* adj_nseg = nullptr;
+  double* adj_segbuf = nullptr;
+  double* adj_stepbuf = nullptr;
+  int adj_k = 0;
+  int adj_w_end = 0;
+  int adj_lanes_blocks = 0;
+  int adj_step_cap = 0;
+  bool adj_recorded = false;
 };
 
 namespace {
@@ -533,6 +549,13 @@ void st_destroy(st_ctx* c) {
   cudaFree(c->sets_d);
   cudaFree(c->status_d);
   cudaFree(c->order_d);
+  cudaFree(c->adj_pool);
+  cudaFree(c->adj_head);
+  cudaFree(c->adj_overflow);
+  cudaFree(c->adj_last);
+  cudaFree(c->adj_nseg);
+  cudaFree(c->adj_segbuf);
+  cudaFree(c->adj_stepbuf);
   if (c->status_h) cudaFreeHost(c->status_h);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -547,6 +570,8 @@ int st_init(st_ctx* c) {
   ST_CUDA(cudaStreamSynchronize(c->stream));
   c->initialized = true;
   c->window_grid = true;
+  c->fresh = true;
+  c->adj_recorded = false;
   return ST_OK;
 }
 
@@ -556,6 +581,8 @@ int st_run_until(st_ctx* c, double next_t) {
   ST_TRY(begin_run(c));
   st::RunArgs a = make_args(c, 0, 0, nullptr);
   ST_TRY(arm_deadline(c, a));
+  c->fresh = false;
+  c->adj_recorded = false;
   int e = st::launch_until(a, next_t, plain_block(c), c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("plain launch: ") + cudaGetErrorString((cudaError_t)e));
   c->window_grid = false;
@@ -569,6 +596,8 @@ int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
   if (w_begin < 0 || w_end < w_begin) return fail(ST_ERR_ARG, "bad window range");
   if (w_end == w_begin) return ST_OK;
   ST_TRY(begin_run(c));
+  c->fresh = false;
+  c->adj_recorded = false;
   int launches = 0;
   if (kernel == ST_KERNEL_PLAIN) {
     st::RunArgs a = make_args(c, w_begin, w_end, snap);
@@ -624,6 +653,18 @@ int st_read_state(st_ctx* c, const st_state_view* h) {
   if (h->n_coll) ST_TRY(get(c->s.n_coll, h->n_coll, 8 * n));
   if (h->n_bounce) ST_TRY(get(c->s.n_bounce, h->n_bounce, 8 * n));
   if (h->n_steps) ST_TRY(get(c->s.n_steps, h->n_steps, 8 * n));
+  return ST_OK;
+}
+
+int st_gather_spins(st_ctx* c, double* dst) {
+  if (!c || !dst) return fail(ST_ERR_ARG, "null argument");
+  ST_CUDA(cudaSetDevice(c->device));
+  if (c->n == 0) return ST_OK;
+  const double* src[3] = {c->s.Sx, c->s.Sy, c->s.Sz};
+  for (int k = 0; k < 3; ++k)
+    ST_CUDA(cudaMemcpy2DAsync(dst + k, 3 * sizeof(double), src[k], sizeof(double), sizeof(double), (size_t)c->n,
+                              cudaMemcpyDeviceToDevice, c->stream));
+  ST_CUDA(cudaStreamSynchronize(c->stream));
   return ST_OK;
 }
 
@@ -702,6 +743,101 @@ int st_get_counters(const st_ctx* c, st_counters* out) {
   if (!c || !out) return fail(ST_ERR_ARG, "null argument");
   *out = c->last;
   return ST_OK;
+}
+
+int st_adjoint_record(st_ctx* c, int w_end, int segments_per_checkpoint, size_t pool_bytes) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  if (!c->fresh) return fail(ST_ERR_STATE, "st_adjoint_record needs a freshly initialised context (st_init)");
+  if (w_end < 0) return fail(ST_ERR_ARG, "negative window count");
+#if !ST_GRAD_IS_LINEAR
+  return fail(ST_ERR_UNSUPPORTED, "the adjoint needs the linear grad hook (ST_GRAD_IS_LINEAR)");
+#endif
+  for (const auto& P : c->sets_h)
+    if (P.integrator != 0) return fail(ST_ERR_UNSUPPORTED, "the adjoint differentiates DOP853 (integratorType 0) only");
+  ST_CUDA(cudaSetDevice(c->device));
+  const int k = segments_per_checkpoint > 0 ? segments_per_checkpoint : 64;
+  const size_t n = (size_t)std::max<int64_t>(c->n, 1);
+  if (!c->adj_last) {
+    ST_CUDA(cudaMalloc(&c->adj_last, 8 * n));
+    ST_CUDA(cudaMalloc(&c->adj_nseg, 8 * n));
+    ST_CUDA(cudaMalloc(&c->adj_head, sizeof(unsigned long long)));
+    ST_CUDA(cudaMalloc(&c->adj_overflow, sizeof(int)));
+  }
+  size_t want = pool_bytes;
+  if (want == 0) {
+    size_t free_b = 0, total_b = 0;
+    ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    want = free_b / 4;
+  }
+  const int64_t cap = (int64_t)(want / st::adj_ckpt_bytes());
+  if (cap < 1) return fail(ST_ERR_ARG, "checkpoint pool too small");
+  if (cap != c->adj_pool_cap) {
+    cudaFree(c->adj_pool);
+    c->adj_pool = nullptr;
+    cudaError_t e = cudaMalloc(&c->adj_pool, (size_t)cap * st::adj_ckpt_bytes());
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("checkpoint pool: ") + cudaGetErrorString(e));
+    c->adj_pool_cap = cap;
+  }
+  ST_TRY(begin_run(c));
+  ST_CUDA(cudaMemsetAsync(c->adj_head, 0, sizeof(unsigned long long), c->stream));
+  ST_CUDA(cudaMemsetAsync(c->adj_overflow, 0, sizeof(int), c->stream));
+  st::RunArgs a = make_args(c, 0, w_end, nullptr);
+  st::AdjArgs b{};
+  b.pool = (st::Ckpt*)c->adj_pool;
+  b.pool_head = c->adj_head;
+  b.pool_cap = c->adj_pool_cap;
+  b.last_ckpt = c->adj_last;
+  b.nseg = c->adj_nseg;
+  b.k = k;
+  b.overflow = c->adj_overflow;
+  int e = st::launch_adj_record(a, b, c->sm_count * 8, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("adjoint record launch: ") + cudaGetErrorString((cudaError_t)e));
+  int over = 0;
+  ST_CUDA(cudaMemcpyAsync(&over, c->adj_overflow, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ST_TRY(end_run(c, 1));
+  c->fresh = false;
+  c->window_grid = true;
+  if (over) return fail(ST_ERR_NOMEM, "checkpoint pool exhausted: raise pool_bytes or segments_per_checkpoint");
+  c->adj_k = k;
+  c->adj_w_end = w_end;
+  c->adj_recorded = true;
+  return ST_OK;
+}
+
+int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags) {
+  if (!c || !dL_dS || !grad) return fail(ST_ERR_ARG, "null argument");
+  if (!c->adj_recorded) return fail(ST_ERR_STATE, "st_adjoint_backward needs st_adjoint_record first");
+  ST_CUDA(cudaSetDevice(c->device));
+  const int blocks = c->sm_count * 2;
+  const int64_t lanes = (int64_t)blocks * 128;
+  const int step_cap = 1024;
+  if (!c->adj_segbuf || c->adj_lanes_blocks != blocks || c->adj_step_cap != step_cap) {
+    cudaFree(c->adj_segbuf);
+    cudaFree(c->adj_stepbuf);
+    c->adj_segbuf = c->adj_stepbuf = nullptr;
+    cudaError_t e = cudaMalloc(&c->adj_segbuf, sizeof(double) * (size_t)lanes * (size_t)c->adj_k * st::kAdjSegF);
+    if (e == cudaSuccess) e = cudaMalloc(&c->adj_stepbuf, sizeof(double) * (size_t)lanes * (size_t)step_cap * 5);
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
+    c->adj_lanes_blocks = blocks;
+    c->adj_step_cap = step_cap;
+  }
+  ST_TRY(begin_run(c));
+  st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
+  st::AdjArgs b{};
+  b.pool = (st::Ckpt*)c->adj_pool;
+  b.pool_cap = c->adj_pool_cap;
+  b.last_ckpt = c->adj_last;
+  b.nseg = c->adj_nseg;
+  b.k = c->adj_k;
+  b.dLdS = dL_dS;
+  b.grad = grad;
+  b.segbuf = c->adj_segbuf;
+  b.stepbuf = c->adj_stepbuf;
+  b.step_cap = step_cap;
+  b.pulse_grads = (flags & 1) ? 1 : 0;
+  int e = st::launch_adj_backward(a, b, blocks, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("adjoint backward launch: ") + cudaGetErrorString((cudaError_t)e));
+  return end_run(c, 1);
 }
 
 int st_probe_fp64_peak(int device, double* tflops) {

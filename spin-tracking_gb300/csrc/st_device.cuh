@@ -427,8 +427,10 @@ struct Seg {
   double t0, xf, x, h, posneg, facold;
   double kx, ky, kz;   // DOP853: derivative at (x, y) (FSAL); RK45: last stage-6 state
   double lastH, lnprev;
+  double hu;           // step size of the last accepted attempt (read by the adjoint replay)
   unsigned int nstep;
   bool reject, last;
+  bool acc;            // the last attempt was accepted
 };
 
 // The per-set field constants (launch_prepare_sets): gamma * B0, the gradient
@@ -563,6 +565,7 @@ __device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& S
   }
   if (h < P.hmin && !last) h = P.hmin;
   g.nstep++;
+  g.acc = false;
   const double tx = g.x - g.t0;
   const double k1x = g.kx, k1y = g.ky, k1z = g.kz;
   double ax, ay, az, yx, yy, yz;
@@ -644,6 +647,8 @@ __device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& S
   }
   int ret = 0;
   if (err <= 1.0 || P.fixed) {
+    g.acc = true;
+    g.hu = h;
     g.facold = max_d(err, 1.0e-4);
     bloch(nx, ny, nz, Ox12, Oy12, Oz12, g.kx, g.ky, g.kz);  // FSAL: f(x + h, y_new)
     Sx = nx; Sy = ny; Sz = nz;

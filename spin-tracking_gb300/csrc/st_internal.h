@@ -94,6 +94,30 @@ struct RunArgs {
   int count_work;                 // accumulate attempt counters
 };
 
+// Discrete adjoint (st_adjoint.cu): gradient of L(S_final) with respect to
+// theta = [Gx(3), Gy(3), Gz(3), B0(3), E(3), a, w].
+constexpr int kNumTheta = 17;
+struct Ckpt;
+struct AdjArgs {
+  Ckpt* pool;                     // checkpoint pool
+  unsigned long long* pool_head;  // bump allocator cursor
+  int64_t pool_cap;
+  int64_t* last_ckpt;             // per particle: its last checkpoint (-1: none)
+  int64_t* nseg;                  // per particle: segments of the record pass
+  int k;                          // segments per checkpoint
+  const double* dLdS;             // per particle, 3 doubles
+  double* grad;                   // per particle, kNumTheta doubles
+  double* segbuf;                 // per lane: k segment records
+  double* stepbuf;                // per lane: step_cap records (y, x, h)
+  int step_cap;
+  int pulse_grads;
+  int* overflow;                  // set when the pool ran out
+};
+int launch_adj_record(const RunArgs& a, const AdjArgs& b, int blocks, void* stream);
+int launch_adj_backward(const RunArgs& a, const AdjArgs& b, int blocks, void* stream);
+size_t adj_ckpt_bytes();
+constexpr int kAdjSegF = 20;      // doubles per segment record of the backward pass
+
 // Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
 // cast to int (0 = success).
 int launch_prepare_sets(SetParams* sets, int nsets, void* stream);

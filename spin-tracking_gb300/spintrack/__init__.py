@@ -156,6 +156,19 @@ class Particles:
         check(load().st_get_counters(self._ctx, ctypes.byref(c)))
         return {k: int(getattr(c, k)) for k, _ in Counters._fields_}
 
+    def gather_spins(self, dst_ptr: int) -> None:
+        """Copy the spins into a dense device array (3 doubles per particle) at dst_ptr."""
+        check(load().st_gather_spins(self._ctx, ctypes.c_void_p(dst_ptr)))
+
+    def adjoint_record(self, w_end: int, segments_per_checkpoint: int = 0, pool_bytes: int = 0) -> None:
+        """Forward pass with checkpoints for adjoint_backward (needs a fresh init_particles)."""
+        check(load().st_adjoint_record(self._ctx, int(w_end), int(segments_per_checkpoint), int(pool_bytes)))
+
+    def adjoint_backward(self, dLdS_ptr: int, grad_ptr: int, pulse: bool = False) -> None:
+        """dL/dS (device, 3 doubles per particle) -> dL/dtheta per particle (device, 17 doubles)."""
+        check(load().st_adjoint_backward(self._ctx, ctypes.c_void_p(dLdS_ptr), ctypes.c_void_p(grad_ptr),
+                                         1 if pulse else 0))
+
     def stream(self) -> int:
         """The context's cudaStream_t as an integer handle."""
         return int(load().st_get_stream(self._ctx) or 0)

@@ -88,6 +88,7 @@ _SIGS = {
     "st_snapshot_field_offset": (c_size_t, [c_void_p, c_int]),
     "st_read_state": (c_int, [c_void_p, POINTER(StateView)]),
     "st_device_state": (c_int, [c_void_p, POINTER(DeviceSoA)]),
+    "st_gather_spins": (c_int, [c_void_p, c_void_p]),
     "st_synchronize": (c_int, [c_void_p]),
     "st_get_stream": (c_void_p, [c_void_p]),
     "st_set_params": (c_int, [c_void_p, POINTER(Options), c_int]),
@@ -100,6 +101,8 @@ _SIGS = {
     "st_get_counters": (c_int, [c_void_p, POINTER(Counters)]),
     "st_main_analysis": (c_int, [POINTER(Options), c_char_p, c_int, c_int, POINTER(c_double)]),
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),
+    "st_adjoint_record": (c_int, [c_void_p, c_int, c_int, c_size_t]),
+    "st_adjoint_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     "st_run_noalloc": (c_int, [POINTER(Options), c_int, c_void_p, POINTER(c_size_t), c_int, c_void_p]),
     "st_write_header": (c_int, [c_void_p, POINTER(Options)]),
     "st_write_snapshot": (c_int, [c_void_p, c_int, POINTER(StateView)]),

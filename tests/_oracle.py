@@ -71,6 +71,8 @@ class Oracle:
             "or_main_analysis": (c_int, [P(Options), ctypes.c_char_p, c_int, P(c_double)]),
             "or_run_sample": (c_double, [P(Options), c_int, c_int, c_int, P(Particles)]),
             "or_set_counters": (None, [c_void_p]),
+            "or_set_step_log": (None, [c_void_p, ctypes.c_int64, c_int]),
+            "or_step_log_count": (ctypes.c_int64, []),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
