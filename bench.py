@@ -176,6 +176,46 @@ def cpu_sample_rate(tf: float, target_s: float, first: int = 0):
     return n * sim / secs, cores, f"particles [{first}, {first + n}) of the workload, t = 0..{sim:g} s, {secs:.1f} s wall"
 
 
+# ---------------------------------------------------------------- adjoint
+ADJ_WORKLOAD = ("adjoint: 65,536 particles, MB 4.2 K, specular walls, gravity, gas off, full G ~ N(0,1e-9) T/m, "
+                "E=(0,0,75e5), B0=(3e-6,0,0), DOP853 rtol 1e-12, tf = 1 s (shortened from 50 s), gradients of "
+                "<Sx> w.r.t. G(9), B0(3), E(3); checkpoint every 64 segments")
+
+
+def adjoint_timing(args, dev):
+    import torch
+    import spintrack as st
+    g = np.random.default_rng(0).normal(0.0, 1e-9, 9)
+    n = 65536
+    opt = st.derive(st.make_options(numParticles=n, dist="M", T=4.2, diffuse=0.0, gas_coll=False, gravity=True,
+                                    Gx=g[0:3], Gy=g[3:6], Gz=g[6:9], E=(0, 0, 75e5), B0=(3e-6, 0, 0), yi=(0, 0, 1),
+                                    tf=1.0, ioutInt=0.5, seed=0))
+    nw = st.num_windows(opt)
+    with st.Particles(opt, device=dev) as p:
+        def timed(fn):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0
+        p.init_particles()
+        p.run_windows(0, nw, st.KERNEL_PERSISTENT)
+        p.init_particles()
+        t_fwd = timed(lambda: p.run_windows(0, nw, st.KERNEL_PERSISTENT))
+        p.init_particles()
+        t_rec = timed(lambda: p.adjoint_record(nw, 64))
+        w = torch.zeros(n, 3, dtype=torch.float64, device=f"cuda:{dev}")
+        w[:, 0] = 1.0 / n
+        out = torch.empty(n, 17, dtype=torch.float64, device=f"cuda:{dev}")
+        t_bwd = timed(lambda: p.adjoint_backward(w.data_ptr(), out.data_ptr()))
+        finite = bool(torch.isfinite(out).all().item())
+        del w, out
+        torch.cuda.synchronize()
+    return {"workload": ADJ_WORKLOAD, "forward_batched_s": t_fwd, "record_s": t_rec, "backward_s": t_bwd,
+            "backward_over_forward": t_bwd / t_fwd, "record_plus_backward_over_forward": (t_rec + t_bwd) / t_fwd,
+            "gradients_finite": finite}
+
+
 # ---------------------------------------------------------------- main
 def run_reference(args, world, rank):
     if rank != 0:
@@ -314,6 +354,12 @@ def run_ours(args, world, rank, local):
     e2e = {"value": n_total * sim / te, "unit": UNIT, "h2d_bytes_per_step": p.param_table_bytes() * world,
            "d2h_bytes_per_step": int(snap.numel()) * world, "ms_per_step": te * 1e3}
 
+    # ---- discrete adjoint on the adjoint workload shape (65,536 particles,
+    # specular walls, tf = 1 s): record pass + backward vs a forward pass
+    adjoint = None
+    if not args.skip_adjoint and rank == 0:
+        adjoint = adjoint_timing(args, dev)
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         rate, cores, sample = cpu_sample_rate(args.tf, args.cpu_seconds)
@@ -336,7 +382,7 @@ def run_ours(args, world, rank, local):
                            "kernel": args.kernel, "launch_config": {"variant": lcfg[0], "blocks_per_sm": lcfg[1]},
                            "l2": "inputs larger than L2: per-particle state 178 MB + snapshot blocks, rewritten each step",
                            "parallelism": f"particle shards x{world}"},
-                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain_kernel": plain,
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain_kernel": plain, "adjoint": adjoint,
                 "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line), flush=True)
     return 0
@@ -355,6 +401,7 @@ def main():
     ap.add_argument("--bps", type=int, default=0, help="resident blocks per SM with --variant")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     args = ap.parse_args()

@@ -169,12 +169,13 @@ __global__ void k_adj_record(RunArgs a, AdjArgs b) {
 
 // ---------------------------------------------------------------- adjoint step
 namespace adj {
-// stage inputs: for stage s (2..12) the earlier stages it sums and their coefficients
-__device__ __constant__ int kLst[13][9] = {
+// stage inputs: for stage s (2..12) the earlier stages it sums and their
+// coefficients; compile-time tables so every index resolves to a register
+constexpr __device__ int kLst[13][9] = {
     {0}, {0}, {1}, {1, 2}, {1, 3}, {1, 3, 4}, {1, 4, 5}, {1, 4, 5, 6}, {1, 4, 5, 6, 7}, {1, 4, 5, 6, 7, 8},
     {1, 4, 5, 6, 7, 8, 9}, {1, 4, 5, 6, 7, 8, 9, 10}, {1, 4, 5, 6, 7, 8, 9, 10, 11}};
-__device__ __constant__ int kCnt[13] = {0, 0, 1, 2, 2, 3, 3, 4, 5, 6, 7, 8, 9};
-__device__ __constant__ double kA[13][9] = {
+constexpr __device__ int kCnt[13] = {0, 0, 1, 2, 2, 3, 3, 4, 5, 6, 7, 8, 9};
+constexpr __device__ double kA[13][9] = {
     {0}, {0}, {dop::A21}, {dop::A31, dop::A32}, {dop::A41, dop::A43}, {dop::A51, dop::A53, dop::A54},
     {dop::A61, dop::A64, dop::A65}, {dop::A71, dop::A74, dop::A75, dop::A76},
     {dop::A81, dop::A84, dop::A85, dop::A86, dop::A87},
@@ -183,11 +184,11 @@ __device__ __constant__ double kA[13][9] = {
     {dop::A111, dop::A114, dop::A115, dop::A116, dop::A117, dop::A118, dop::A119, dop::A1110},
     {dop::A121, dop::A124, dop::A125, dop::A126, dop::A127, dop::A128, dop::A129, dop::A1210, dop::A1211}};
 // node of stage s (stage 12 at x + h)
-__device__ __constant__ double kC[13] = {0, 0, dop::C2, dop::C3, dop::C4, dop::C5, dop::C6, dop::C7, dop::C8,
-                                         dop::C9, dop::C10, dop::C11, 1.0};
+constexpr __device__ double kC[13] = {0, 0, dop::C2, dop::C3, dop::C4, dop::C5, dop::C6, dop::C7, dop::C8,
+                                      dop::C9, dop::C10, dop::C11, 1.0};
 // 8th-order weights per stage
-__device__ __constant__ double kB[13] = {0, dop::B1, 0, 0, 0, 0, dop::B6, dop::B7, dop::B8, dop::B9, dop::B10,
-                                         dop::B11, dop::B12};
+constexpr __device__ double kB[13] = {0, dop::B1, 0, 0, 0, 0, dop::B6, dop::B7, dop::B8, dop::B9, dop::B10,
+                                      dop::B11, dop::B12};
 }  // namespace adj
 
 struct Moments {
@@ -201,51 +202,66 @@ __device__ __forceinline__ void cross3(const double a[3], const double b[3], dou
   r[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+__device__ __forceinline__ double stage_tau(int s, double tx, double h) {
+  return (s == 1) ? tx : (s == 12 ? tx + h : fma(adj::kC[s], h, tx));
+}
+
 // Backward through one accepted DOP853 step from (x, y) with step h:
 // lam (adjoint of the step's result) becomes the adjoint of y; the stages'
-// dL/dOmega are accumulated into the segment moments.
-__device__ void dop_step_adjoint(const Seg& g, const SetParams& P, double x, double h, const double y[3],
-                                 double lam[3], Moments& M, bool pulse) {
-  double Y[13][3], K[13][3], tau[13];
+// dL/dOmega are accumulated into the segment moments.  The 12 stage states go
+// to shared memory (ysm[(s * 3 + c) * BLOCK]), the stage derivatives and their
+// adjoints stay in registers.
+template <int BLOCK>
+__device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& P, double x, double h, const double y[3],
+                                                 double lam[3], Moments& M, bool pulse, double* sm) {
+  // sm[((s - 1) * 3 + c) * BLOCK]: stage state yy_s; sm[(36 + (s - 1) * 3 + c) * BLOCK]: k_s
+#define ST_YS(s, c) sm[(((s)-1) * 3 + (c)) * BLOCK]
+#define ST_KS(s, c) sm[(36 + ((s)-1) * 3 + (c)) * BLOCK]
   const double tx = x - g.t0;
   // forward recompute of the stages
 #pragma unroll
   for (int s = 1; s <= 12; ++s) {
-    tau[s] = (s == 1) ? tx : (s == 12 ? tx + h : fma(adj::kC[s], h, tx));
+    double Y[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       double acc = 0.0;
 #pragma unroll
-      for (int j = 0; j < adj::kCnt[s]; ++j) acc = fma(adj::kA[s][j], K[adj::kLst[s][j]][c], acc);
-      Y[s][c] = (s == 1) ? y[c] : fma(h, acc, y[c]);
+      for (int j = 0; j < adj::kCnt[s]; ++j) acc = fma(adj::kA[s][j], ST_KS(adj::kLst[s][j], c), acc);
+      Y[c] = (s == 1) ? y[c] : fma(h, acc, y[c]);
+      ST_YS(s, c) = Y[c];
     }
-    double O[3];
-    omega_at(g, P, tau[s], O[0], O[1], O[2]);
-    bloch(Y[s][0], Y[s][1], Y[s][2], O[0], O[1], O[2], K[s][0], K[s][1], K[s][2]);
+    double O[3], k[3];
+    omega_at(g, P, stage_tau(s, tx, h), O[0], O[1], O[2]);
+    bloch(Y[0], Y[1], Y[2], O[0], O[1], O[2], k[0], k[1], k[2]);
+    ST_KS(s, 0) = k[0];
+    ST_KS(s, 1) = k[1];
+    ST_KS(s, 2) = k[2];
   }
-  // backward: Kb[s] = dL/dk_s
+  // backward: Kb[s] = dL/dk_s, pushed from the later stages
   double Kb[13][3];
 #pragma unroll
   for (int s = 1; s <= 12; ++s)
 #pragma unroll
     for (int c = 0; c < 3; ++c) Kb[s][c] = h * adj::kB[s] * lam[c];
-  double ly[3] = {lam[0], lam[1], lam[2]};
 #pragma unroll
   for (int s = 12; s >= 1; --s) {
+    const double tau = stage_tau(s, tx, h);
     double O[3];
-    omega_at(g, P, tau[s], O[0], O[1], O[2]);
+    omega_at(g, P, tau, O[0], O[1], O[2]);
+    const double Y[3] = {ST_YS(s, 0), ST_YS(s, 1), ST_YS(s, 2)};
     double yb[3], z[3];
-    cross3(O, Kb[s], yb);     // dL/dyy_s = Omega x kbar
-    cross3(Kb[s], Y[s], z);   // dL/dOmega_s = kbar x yy
+    cross3(O, Kb[s], yb);  // dL/dyy_s = Omega x kbar
+    cross3(Kb[s], Y, z);   // dL/dOmega_s = kbar x yy
+    const double tau2 = tau * tau;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       M.z0[c] += z[c];
-      M.z1[c] = fma(z[c], tau[s], M.z1[c]);
-      M.z2[c] = fma(z[c], tau[s] * tau[s], M.z2[c]);
-      ly[c] += yb[c];
+      M.z1[c] = fma(z[c], tau, M.z1[c]);
+      M.z2[c] = fma(z[c], tau2, M.z2[c]);
+      lam[c] += yb[c];
     }
     if (pulse) {
-      const double t = g.t0 + tau[s];
+      const double t = g.t0 + tau;
       double sn, cs;
       sincos(P.w * t, &sn, &cs);
       M.ga = fma(P.gamma * cs, z[2], M.ga);
@@ -259,55 +275,69 @@ __device__ void dop_step_adjoint(const Seg& g, const SetParams& P, double x, dou
       for (int c = 0; c < 3; ++c) Kb[l][c] = fma(ha, yb[c], Kb[l][c]);
     }
   }
-  lam[0] = ly[0];
-  lam[1] = ly[1];
-  lam[2] = ly[2];
+#undef ST_YS
+#undef ST_KS
 }
 
-// Contract a segment's moments into dL/dtheta (theta order of the file header).
+// Contract a segment's moments into dL/dtheta (theta order of the file header);
+// gth is strided by `stride` (shared memory, one column per thread).
 __device__ __forceinline__ void contract(const SetParams& P, const double p0[3], const double v0[3], const Moments& M,
-                                         double gth[kNumTheta]) {
+                                         double* gth, int stride) {
   const double gm = P.gamma;
   const double g_ = P.gravity ? kGravity : 0.0;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-      gth[3 * i + j] += gm * (M.z0[i] * p0[j] + M.z1[i] * v0[j] + (j == 1 ? 0.5 * g_ * M.z2[i] : 0.0));
-    gth[9 + i] += gm * M.z0[i];
+      gth[(3 * i + j) * stride] += gm * (M.z0[i] * p0[j] + M.z1[i] * v0[j] + (j == 1 ? 0.5 * g_ * M.z2[i] : 0.0));
+    gth[(9 + i) * stride] += gm * M.z0[i];
   }
   // E: sum_s z_s x v_s with v_s = v0 + g tau_s yhat
   double zv[3];
   cross3(M.z0, v0, zv);
   const double ci = gm * P.inv_c2;
-  gth[12] += ci * (zv[0] - g_ * M.z1[2]);
-  gth[13] += ci * zv[1];
-  gth[14] += ci * (zv[2] + g_ * M.z1[0]);
-  gth[15] += M.ga;
-  gth[16] += M.gw;
+  gth[12 * stride] += ci * (zv[0] - g_ * M.z1[2]);
+  gth[13 * stride] += ci * zv[1];
+  gth[14 * stride] += ci * (zv[2] + g_ * M.z1[0]);
+  gth[15 * stride] += M.ga;
+  gth[16 * stride] += M.gw;
 }
 
 // ---------------------------------------------------------------- backward
 constexpr int kSegF = kAdjSegF;  // t0 t1 o0[3] o1[3] p0[3] v0[3] y0[3] tempH0 step_start nsteps(-1: not stored, -2: none)
 
-__global__ void k_adj_backward(RunArgs a, AdjArgs b) {
+constexpr int kAdjBlock = 64;
+
+__global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, AdjArgs b) {
+  __shared__ double ysm_all[2 * 12 * 3 * kAdjBlock];  // stage states, then stage derivatives
+  __shared__ double gsm_all[kNumTheta * kAdjBlock];
+  double* ysm = ysm_all + threadIdx.x;
+  double* gth = gsm_all + threadIdx.x;  // gradient accumulators, stride kAdjBlock
   const int64_t nl = (int64_t)gridDim.x * blockDim.x;
   const int64_t lane = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double* sb = b.segbuf + lane * (int64_t)b.k * kSegF;
   double* st = b.stepbuf + lane * (int64_t)b.step_cap * 5;
   for (int64_t i = lane; i < a.s.n; i += nl) {
     const SetParams& P = a.sets[a.s.set[i]];
-    double gth[kNumTheta];
 #pragma unroll
-    for (int q = 0; q < kNumTheta; ++q) gth[q] = 0.0;
+    for (int q = 0; q < kNumTheta; ++q) gth[q * kAdjBlock] = 0.0;
     double lam[3] = {b.dLdS[3 * i], b.dLdS[3 * i + 1], b.dLdS[3 * i + 2]};
     const bool live = a.s.stop[i] == 0 && (lam[0] != 0.0 || lam[1] != 0.0 || lam[2] != 0.0);
     int64_t ck = live ? b.last_ckpt[i] : -1;
     int64_t seg_end = b.nseg[i];
     const int wlast = min(a.w_end, P.nwin);
     while (ck >= 0) {
+      if (ck >= b.pool_cap) {  // corrupt link: record and stop this particle
+        atomicExch(b.overflow, 1);
+        break;
+      }
       const Ckpt C = b.pool[ck];
-      const int nblk = (int)(seg_end - C.seg);
+      const int64_t nblk64 = seg_end - C.seg;
+      if (nblk64 < 0 || nblk64 > b.k) {  // block larger than the per-lane scratch
+        atomicExch(b.overflow, 1);
+        break;
+      }
+      const int nblk = (int)nblk64;
       // -- replay the block: segment descriptors, and the steps while they fit
       Walker W;
       ckpt_read(C, W, wlast);
@@ -367,7 +397,7 @@ __global__ void k_adj_backward(RunArgs a, AdjArgs b) {
           for (int k = ns - 1; k >= 0; --k) {
             const double* e = st + (int64_t)(s0 + k) * 5;
             const double y[3] = {e[0], e[1], e[2]};
-            dop_step_adjoint(g, P, e[3], e[4], y, lam, M, b.pulse_grads != 0);
+            dop_step_adjoint<kAdjBlock>(g, P, e[3], e[4], y, lam, M, b.pulse_grads != 0, ysm);
           }
         } else {
           // steps did not fit: replay this segment alone, in chunks of step_cap
@@ -404,19 +434,19 @@ __global__ void k_adj_backward(RunArgs a, AdjArgs b) {
             for (int k = hi - lo - 1; k >= 0; --k) {
               const double* e = wk + (int64_t)k * 5;
               const double y[3] = {e[0], e[1], e[2]};
-              dop_step_adjoint(g, P, e[3], e[4], y, lam, M, b.pulse_grads != 0);
+              dop_step_adjoint<kAdjBlock>(g, P, e[3], e[4], y, lam, M, b.pulse_grads != 0, ysm);
             }
           }
         }
         const double p0[3] = {d[8], d[9], d[10]};
         const double v0[3] = {d[11], d[12], d[13]};
-        contract(P, p0, v0, M, gth);
+        contract(P, p0, v0, M, gth, kAdjBlock);
       }
       seg_end = C.seg;
       ck = C.prev;
     }
 #pragma unroll
-    for (int q = 0; q < kNumTheta; ++q) b.grad[i * kNumTheta + q] = gth[q];
+    for (int q = 0; q < kNumTheta; ++q) b.grad[i * kNumTheta + q] = gth[q * kAdjBlock];
   }
 }
 
@@ -429,7 +459,7 @@ int launch_adj_record(const RunArgs& a, const AdjArgs& b, int blocks, void* stre
 
 int launch_adj_backward(const RunArgs& a, const AdjArgs& b, int blocks, void* stream) {
   if (a.s.n == 0) return 0;
-  k_adj_backward<<<blocks, 128, 0, (cudaStream_t)stream>>>(a, b);
+  k_adj_backward<<<blocks, kAdjBlock, 0, (cudaStream_t)stream>>>(a, b);
   return (int)cudaGetLastError();
 }
 

@@ -180,6 +180,7 @@ struct st_ctx {
   int adj_w_end = 0;
   int adj_lanes_blocks = 0;
   int adj_step_cap = 0;
+  int adj_seg_k = 0;         // segments per lane the backward scratch was sized for
   bool adj_recorded = false;
 };
 
@@ -811,7 +812,7 @@ int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags)
   const int blocks = c->sm_count * 2;
   const int64_t lanes = (int64_t)blocks * 128;
   const int step_cap = 1024;
-  if (!c->adj_segbuf || c->adj_lanes_blocks != blocks || c->adj_step_cap != step_cap) {
+  if (!c->adj_segbuf || c->adj_lanes_blocks != blocks || c->adj_step_cap != step_cap || c->adj_seg_k != c->adj_k) {
     cudaFree(c->adj_segbuf);
     cudaFree(c->adj_stepbuf);
     c->adj_segbuf = c->adj_stepbuf = nullptr;
@@ -820,6 +821,7 @@ int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags)
     if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
     c->adj_lanes_blocks = blocks;
     c->adj_step_cap = step_cap;
+    c->adj_seg_k = c->adj_k;
   }
   ST_TRY(begin_run(c));
   st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
@@ -835,9 +837,15 @@ int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags)
   b.stepbuf = c->adj_stepbuf;
   b.step_cap = step_cap;
   b.pulse_grads = (flags & 1) ? 1 : 0;
+  b.overflow = c->adj_overflow;
+  ST_CUDA(cudaMemsetAsync(c->adj_overflow, 0, sizeof(int), c->stream));
   int e = st::launch_adj_backward(a, b, blocks, c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("adjoint backward launch: ") + cudaGetErrorString((cudaError_t)e));
-  return end_run(c, 1);
+  int bad = 0;
+  ST_CUDA(cudaMemcpyAsync(&bad, c->adj_overflow, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ST_TRY(end_run(c, 1));
+  if (bad) return fail(ST_ERR_CUDA, "internal: an adjoint block was larger than its scratch (skipped)");
+  return ST_OK;
 }
 
 int st_probe_fp64_peak(int device, double* tflops) {

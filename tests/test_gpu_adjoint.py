@@ -149,3 +149,25 @@ def test_ensemble_losses_backpropagate(gpu):
     eng.close()
     assert torch.allclose(g1[0], g2, rtol=1e-12, atol=0.0)
     assert torch.all(torch.isfinite(g1))
+
+
+def test_backward_after_changing_checkpoint_spacing(gpu):
+    """Record passes with different segments-per-checkpoint on one context
+    (the backward scratch is resized); gradients agree across spacings."""
+    import torch
+    opt = adj_options(n=16, tf=0.1)
+    nw = st.num_windows(opt)
+    dev = torch.device("cuda", 0)
+    grads = []
+    with st.Particles(opt) as p:
+        for k in (4, 64, 256):
+            p.init_particles()
+            p.adjoint_record(nw, segments_per_checkpoint=k)
+            w = torch.zeros(opt.numParticles, 3, dtype=torch.float64, device=dev)
+            w[:, 0] = 1.0
+            out = torch.empty(opt.numParticles, NUM_THETA, dtype=torch.float64, device=dev)
+            torch.cuda.synchronize()
+            p.adjoint_backward(w.data_ptr(), out.data_ptr())
+            grads.append(out.sum(0).cpu().numpy())
+    for g in grads[1:]:
+        np.testing.assert_allclose(g, grads[0], rtol=1e-12, atol=0.0)
