@@ -199,18 +199,35 @@ int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state
 #define ST_NUM_THETA 17
 /* Forward pass for st_adjoint_backward, from a freshly initialised context
  * (st_init): advances every particle through windows [0, w_end) exactly as
- * st_run_windows does, and stores a full-state checkpoint every
- * segments_per_checkpoint trajectory segments (0 = 64) in a device pool of
- * pool_bytes (0 = a quarter of free device memory).  ST_ERR_NOMEM if the pool
- * runs out.  DOP853 sets only.  No counterpart in the reference (it has no
- * derivatives); the forward arithmetic is the engine's own. */
-int st_adjoint_record(st_ctx *ctx, int w_end, int segments_per_checkpoint, size_t pool_bytes);
+ * st_run_windows does (the trajectory-ahead kernel), and writes the adjoint's
+ * tape: every accepted DOP853 step (y, x, h) and every integrated segment
+ * (t0, p0, v0) of every particle, in pages of a device pool of tape_bytes
+ * (0 = up to 45% of free device memory).  It also keeps a full-state
+ * checkpoint every windows_per_checkpoint windows (0 = chosen so the
+ * checkpoints take at most 10% of free memory).  When the tape does not fit
+ * the pool, st_adjoint_backward replays window chunks from the checkpoints
+ * (and, if one window's tape does not fit, groups of particles), so results
+ * do not depend on the pool size.  DOP853 sets and the linear grad hook only.
+ * No counterpart in the reference (it has no derivatives). */
+int st_adjoint_record(st_ctx *ctx, int w_end, size_t tape_bytes, int windows_per_checkpoint);
 /* Backward pass: given dL/dS_final for every particle (device array,
  * 3 doubles per particle, set order), writes dL/dtheta per particle (device
  * array, ST_NUM_THETA doubles per particle); sum over a set's particles for
  * the set's gradient.  Particles that stopped (failure codes) get zeros.
  * flags bit 0: also differentiate the pulse (a, w), one sincos per stage. */
 int st_adjoint_backward(st_ctx *ctx, const double *dL_dS, double *grad, int flags);
+/* What the last record / backward pair did (no reference counterpart). */
+typedef struct {
+  uint64_t tape_bytes_used;   /* tape written by the record pass (all of it, stored or not) */
+  uint64_t tape_bytes_pool;   /* size of the tape pool */
+  int32_t resident;           /* 1: the record pass's tape fitted, the backward needs no replay */
+  int32_t checkpoints;        /* state checkpoints kept by the record pass */
+  int32_t windows_per_checkpoint;
+  int32_t replays;            /* replay launches of the last backward */
+  int32_t groups;             /* particle-group replays among them */
+  int32_t pad;
+} st_adjoint_stats;
+int st_adjoint_get_stats(const st_ctx *ctx, st_adjoint_stats *out);
 
 /* FP64 FMA issue-rate probe (TFLOP/s, FMA = 2 flops): eight independent
  * DFMA chains per thread on every SM.  No counterpart in the reference; it is

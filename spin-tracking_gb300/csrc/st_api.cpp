@@ -167,34 +167,40 @@ struct st_ctx {
   st_counters last{};
   st::SnapLayout snap{};
   bool fresh = false;        // st_init ran and no run call since
+  size_t arena_bytes = 0;    // bytes of one particle-state arena (state_layout)
   // adjoint (allocated by st_adjoint_record)
-  void* adj_pool = nullptr;
-  int64_t adj_pool_cap = 0;
-  unsigned long long* adj_head = nullptr;
-  int* adj_overflow = nullptr;
-  int64_t* adj_last = nullptr;
-  int64_t* adj_nseg = nullptr;
-  double* adj_segbuf = nullptr;
-  double* adj_stepbuf = nullptr;
-  int adj_k = 0;
+  double* tape_pool = nullptr;
+  int32_t* tape_prev = nullptr;
+  int64_t tape_pages = 0;
+  void* tape_pp = nullptr;   // per-particle tape arrays, lam and work orders
+  unsigned long long* tape_head = nullptr;
+  int* tape_error = nullptr;
+  st::TapeArgs tape{};       // pointers into the above
+  int64_t* adj_order = nullptr;   // every particle, longest tape first
+  int64_t* adj_gorder = nullptr;  // a group of particles replayed together
+  void* ckpt_arena = nullptr;     // state checkpoints, ckpt_count arenas
+  int ckpt_alloc = 0;
+  int ckpt_every = 0, ckpt_count = 0;
+  void* replay_arena = nullptr;   // state of a replay
+  std::vector<int64_t> adj_nsteps_h, adj_nsegs_h;
+  std::vector<uint8_t> adj_stop_h;
   int adj_w_end = 0;
-  int adj_lanes_blocks = 0;
-  int adj_step_cap = 0;
-  int adj_seg_k = 0;         // segments per lane the backward scratch was sized for
+  int adj_w_run = 0;              // windows the record pass ran (w_end capped at the sets' windows)
   bool adj_recorded = false;
+  bool adj_resident = false;      // the record pass's tape is complete and still in the pool
+  st_adjoint_stats adj_stats{};
 };
 
 namespace {
 
-int ctx_alloc(st_ctx* c) {
-  const int64_t n = c->n;
+// Field layout of one particle-state arena: every SoA array 256-byte
+// aligned, in a fixed order.  base == nullptr only computes the size.
+size_t state_layout(st::DeviceState& s, char* base, int64_t n) {
   const size_t m = (size_t)std::max<int64_t>(n, 1);
-  // one arena for every per-particle array, each 256-byte aligned
   struct Field {
     void** ptr;
     size_t elem;
   };
-  st::DeviceState& s = c->s;
   Field f[] = {{(void**)&s.t, 8},        {(void**)&s.px, 8},   {(void**)&s.py, 8},     {(void**)&s.pz, 8},
                {(void**)&s.vx, 8},       {(void**)&s.vy, 8},   {(void**)&s.vz, 8},     {(void**)&s.Sx, 8},
                {(void**)&s.Sy, 8},       {(void**)&s.Sz, 8},   {(void**)&s.h, 8},      {(void**)&s.next_gas, 8},
@@ -202,15 +208,24 @@ int ctx_alloc(st_ctx* c) {
                {(void**)&s.rspare, 8},   {(void**)&s.rhas, 1}, {(void**)&s.fail, 4},   {(void**)&s.n_coll, 8},
                {(void**)&s.n_bounce, 8}, {(void**)&s.n_steps, 8}, {(void**)&s.stop, 1}, {(void**)&s.coll, 1},
                {(void**)&s.wall, 1},     {(void**)&s.set, 4},  {(void**)&s.w_done, 4}};
-  size_t total = 0;
-  for (auto& x : f) total += align256(x.elem * m);
+  size_t off = 0;
+  for (auto& x : f) {
+    *x.ptr = base ? base + off : nullptr;
+    off += align256(x.elem * m);
+  }
+  s.n = n;
+  return off;
+}
+
+int ctx_alloc(st_ctx* c) {
+  const int64_t n = c->n;
+  const size_t m = (size_t)std::max<int64_t>(n, 1);
+  st::DeviceState& s = c->s;
+  const size_t total = state_layout(s, nullptr, n);
   cudaError_t e = cudaMalloc(&c->arena, total);
   if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("cudaMalloc state: ") + cudaGetErrorString(e));
-  char* p = (char*)c->arena;
-  for (auto& x : f) {
-    *x.ptr = p;
-    p += align256(x.elem * m);
-  }
+  state_layout(s, (char*)c->arena, n);
+  c->arena_bytes = total;
   s.n = n;
   ST_CUDA(cudaMemsetAsync(c->arena, 0, total, c->stream));
   // set index of every particle
@@ -266,6 +281,7 @@ st::RunArgs make_args(st_ctx* c, int w_begin, int w_end, void* snap) {
   a.sets = c->sets_d;
   a.nsets = (int)c->sets_h.size();
   a.order = c->order_d;
+  a.nitems = c->n;
   a.s = c->s;
   a.status = c->status_d;
   a.snap = (char*)snap;
@@ -550,13 +566,13 @@ void st_destroy(st_ctx* c) {
   cudaFree(c->sets_d);
   cudaFree(c->status_d);
   cudaFree(c->order_d);
-  cudaFree(c->adj_pool);
-  cudaFree(c->adj_head);
-  cudaFree(c->adj_overflow);
-  cudaFree(c->adj_last);
-  cudaFree(c->adj_nseg);
-  cudaFree(c->adj_segbuf);
-  cudaFree(c->adj_stepbuf);
+  cudaFree(c->tape_pool);
+  cudaFree(c->tape_prev);
+  cudaFree(c->tape_pp);
+  cudaFree(c->tape_head);
+  cudaFree(c->tape_error);
+  cudaFree(c->ckpt_arena);
+  cudaFree(c->replay_arena);
   if (c->status_h) cudaFreeHost(c->status_h);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -746,62 +762,307 @@ int st_get_counters(const st_ctx* c, st_counters* out) {
   return ST_OK;
 }
 
-int st_adjoint_record(st_ctx* c, int w_end, int segments_per_checkpoint, size_t pool_bytes) {
+// ==================================================================== adjoint
+namespace {
+
+constexpr size_t kPageBytes = sizeof(double) * st::kTapePageD;
+
+// Pages a particle's tape needs for n steps and m segments.
+inline int64_t tape_pages_for(int64_t steps, int64_t segs) {
+  return (steps + st::kTapeStepsPerPage - 1) / st::kTapeStepsPerPage +
+         (segs + st::kTapeSegsPerPage - 1) / st::kTapeSegsPerPage;
+}
+
+// Per-particle arrays of the tape (one allocation for the context's life).
+int adj_alloc_particle_arrays(st_ctx* c) {
+  if (c->tape_pp) return ST_OK;
+  const size_t m = (size_t)std::max<int64_t>(c->n, 1);
+  const size_t sz[] = {4 * m, 4 * m, 4 * m, 4 * m, 4 * m, 8 * m, 8 * m, 24 * m, 8 * m, 8 * m};
+  size_t total = 0;
+  for (size_t x : sz) total += align256(x);
+  cudaError_t e = cudaMalloc(&c->tape_pp, total);
+  if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint arrays: ") + cudaGetErrorString(e));
+  char* p = (char*)c->tape_pp;
+  void* ptr[10];
+  for (int k = 0; k < 10; ++k) {
+    ptr[k] = p;
+    p += align256(sz[k]);
+  }
+  st::TapeArgs& t = c->tape;
+  t.step_page = (int32_t*)ptr[0];
+  t.step_fill = (int32_t*)ptr[1];
+  t.seg_page = (int32_t*)ptr[2];
+  t.seg_fill = (int32_t*)ptr[3];
+  t.complete = (int32_t*)ptr[4];
+  t.nsteps = (int64_t*)ptr[5];
+  t.nsegs = (int64_t*)ptr[6];
+  t.lam = (double*)ptr[7];
+  c->adj_order = (int64_t*)ptr[8];
+  c->adj_gorder = (int64_t*)ptr[9];
+  ST_CUDA(cudaMalloc(&c->tape_head, sizeof(unsigned long long)));
+  ST_CUDA(cudaMalloc(&c->tape_error, sizeof(int)));
+  t.pool_head = c->tape_head;
+  t.error = c->tape_error;
+  return ST_OK;
+}
+
+// Clear the per-particle chain heads and the pool cursor before a tape pass.
+int adj_reset_tape(st_ctx* c) {
+  const size_t m = (size_t)std::max<int64_t>(c->n, 1);
+  st::TapeArgs& t = c->tape;
+  ST_CUDA(cudaMemsetAsync(t.step_page, 0xff, 4 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(t.seg_page, 0xff, 4 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(t.step_fill, 0, 4 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(t.seg_fill, 0, 4 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(t.complete, 0, 4 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(t.nsteps, 0, 8 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(t.nsegs, 0, 8 * m, c->stream));
+  ST_CUDA(cudaMemsetAsync(c->tape_head, 0, sizeof(unsigned long long), c->stream));
+  ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(int), c->stream));
+  return ST_OK;
+}
+
+int adj_tape_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) {
+  const int per_sm = std::max(1, st::tape_record_max_blocks_per_sm());
+  int e = st::launch_tape_record(a, t, c->sm_count * per_sm, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("adjoint tape launch: ") + cudaGetErrorString((cudaError_t)e));
+  return ST_OK;
+}
+
+int adj_backward_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) {
+  ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
+  const int per_sm = std::max(1, st::adj_backward_max_blocks_per_sm());
+  int e = st::launch_adj_backward(a, t, c->sm_count * per_sm, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("adjoint backward launch: ") + cudaGetErrorString((cudaError_t)e));
+  int bad = 0;
+  ST_CUDA(cudaMemcpyAsync(&bad, c->tape_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  cudaError_t se = cudaStreamSynchronize(c->stream);
+  if (se != cudaSuccess) return fail(ST_ERR_CUDA, std::string("adjoint backward: ") + cudaGetErrorString(se));
+  if (bad) return fail(ST_ERR_CUDA, "internal: the adjoint tape was inconsistent (code " + std::to_string(bad) + ")");
+  return ST_OK;
+}
+
+// Device state view of a checkpoint slot / the replay scratch.
+st::DeviceState adj_view(st_ctx* c, void* base) {
+  st::DeviceState v{};
+  state_layout(v, (char*)base, c->n);
+  v.set = c->s.set;  // set indices are only kept in the context's own state
+  return v;
+}
+
+// Work order: particles sorted by tape length, longest first, so the lanes
+// that take the last particles finish together.
+int adj_upload_order(st_ctx* c, const std::vector<int64_t>& ids, int64_t* dst) {
+  std::vector<int64_t> o(ids);
+  std::stable_sort(o.begin(), o.end(),
+                   [&](int64_t x, int64_t y) { return c->adj_nsteps_h[(size_t)x] > c->adj_nsteps_h[(size_t)y]; });
+  if (!o.empty())
+    ST_CUDA(cudaMemcpyAsync(dst, o.data(), 8 * o.size(), cudaMemcpyHostToDevice, c->stream));
+  ST_CUDA(cudaStreamSynchronize(c->stream));  // o is freed on return
+  return ST_OK;
+}
+
+// Replay windows up to b_hi from checkpoint slot `slot` for the particles of
+// `group` (nullptr: all), writing their tape; then run the backward over
+// them.  Sets *fitted = false (and runs no backward) when the tape did not fit.
+int adj_replay_and_back(st_ctx* c, int slot, int b_hi, const std::vector<int64_t>* group, const st::TapeArgs& tb,
+                        bool* fitted) {
+  if (group) ST_TRY(adj_upload_order(c, *group, c->adj_gorder));
+  ST_CUDA(cudaMemcpyAsync(c->replay_arena, (char*)c->ckpt_arena + (size_t)slot * c->arena_bytes, c->arena_bytes,
+                          cudaMemcpyDeviceToDevice, c->stream));
+  ST_TRY(adj_reset_tape(c));
+  ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
+  st::RunArgs a = make_args(c, 0, b_hi, nullptr);
+  a.s = adj_view(c, c->replay_arena);
+  a.order = group ? c->adj_gorder : c->order_d;
+  a.nitems = group ? (int64_t)group->size() : c->n;
+  a.count_work = 0;
+  st::TapeArgs t = tb;
+  t.ckpt_every = 0;  // a replay keeps no checkpoints
+  ST_TRY(adj_tape_launch(c, a, t));
+  ++c->adj_stats.replays;
+  // did every particle of the replay store its whole tape?
+  const size_t n = (size_t)c->n;
+  std::vector<int32_t> comp(std::max<size_t>(n, 1));
+  ST_CUDA(cudaMemcpyAsync(comp.data(), t.complete, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  cudaError_t se = cudaStreamSynchronize(c->stream);
+  if (se != cudaSuccess) return fail(ST_ERR_CUDA, std::string("adjoint replay: ") + cudaGetErrorString(se));
+  bool ok = true;
+  const size_t cnt = group ? group->size() : n;
+  for (size_t k = 0; k < cnt && ok; ++k) {
+    const size_t i = group ? (size_t)(*group)[k] : k;
+    if (!c->adj_stop_h[i] && !comp[i]) ok = false;
+  }
+  *fitted = ok;
+  if (!ok) return ST_OK;
+  st::RunArgs ab = make_args(c, 0, b_hi, nullptr);
+  ab.order = group ? c->adj_gorder : c->adj_order;
+  ab.nitems = a.nitems;
+  return adj_backward_launch(c, ab, t);
+}
+
+// One chunk of checkpoint intervals [k_lo, k_hi), last chunk of the run first;
+// split in halves, and single intervals into particle groups, while the tape
+// does not fit.
+int adj_chunk(st_ctx* c, int k_lo, int k_hi, const st::TapeArgs& tb) {
+  const int b_hi = std::min(k_hi * c->ckpt_every, c->adj_w_run);
+  bool fitted = false;
+  ST_TRY(adj_replay_and_back(c, k_lo, b_hi, nullptr, tb, &fitted));
+  if (fitted) return ST_OK;
+  if (k_hi - k_lo > 1) {
+    const int mid = (k_lo + k_hi) / 2;
+    ST_TRY(adj_chunk(c, mid, k_hi, tb));
+    return adj_chunk(c, k_lo, mid, tb);
+  }
+  // one interval whose tape does not fit: groups of particles (the replay
+  // above counted each particle's records for this interval)
+  const size_t n = (size_t)c->n;
+  std::vector<int64_t> ns(n), ng(n);
+  ST_CUDA(cudaMemcpyAsync(ns.data(), tb.nsteps, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaMemcpyAsync(ng.data(), tb.nsegs, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<int64_t> group;
+  int64_t used = 0;
+  auto flush = [&]() -> int {
+    if (group.empty()) return ST_OK;
+    bool ok = false;
+    ++c->adj_stats.groups;
+    ST_TRY(adj_replay_and_back(c, k_lo, b_hi, &group, tb, &ok));
+    if (!ok) return fail(ST_ERR_CUDA, "internal: a particle group's tape did not fit its estimate");
+    group.clear();
+    used = 0;
+    return ST_OK;
+  };
+  for (size_t i = 0; i < n; ++i) {
+    if (c->adj_stop_h[i]) continue;
+    const int64_t need = tape_pages_for(ns[i], ng[i]);
+    if (need > c->tape_pages)
+      return fail(ST_ERR_NOMEM, "one particle's tape over one checkpoint interval is larger than the tape pool: "
+                                "raise tape_bytes or lower windows_per_checkpoint");
+    if (used + need > c->tape_pages) ST_TRY(flush());
+    group.push_back((int64_t)i);
+    used += need;
+  }
+  return flush();
+}
+
+st::TapeArgs adj_tape_args(st_ctx* c) {
+  st::TapeArgs t = c->tape;
+  t.pool = c->tape_pool;
+  t.page_prev = c->tape_prev;
+  t.pool_pages = c->tape_pages;
+  t.ckpt = adj_view(c, c->ckpt_arena);
+  t.ckpt_stride = (int64_t)c->arena_bytes;
+  t.ckpt_every = c->ckpt_every;
+  t.ckpt_count = c->ckpt_count;
+  return t;
+}
+
+}  // namespace
+
+int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_checkpoint) {
   if (!c) return fail(ST_ERR_ARG, "null context");
   if (!c->fresh) return fail(ST_ERR_STATE, "st_adjoint_record needs a freshly initialised context (st_init)");
   if (w_end < 0) return fail(ST_ERR_ARG, "negative window count");
+  if (windows_per_checkpoint < 0) return fail(ST_ERR_ARG, "negative windows_per_checkpoint");
 #if !ST_GRAD_IS_LINEAR
   return fail(ST_ERR_UNSUPPORTED, "the adjoint needs the linear grad hook (ST_GRAD_IS_LINEAR)");
 #endif
-  for (const auto& P : c->sets_h)
+  int nwin_max = 0;
+  for (const auto& P : c->sets_h) {
     if (P.integrator != 0) return fail(ST_ERR_UNSUPPORTED, "the adjoint differentiates DOP853 (integratorType 0) only");
+    nwin_max = std::max(nwin_max, P.nwin);
+  }
   ST_CUDA(cudaSetDevice(c->device));
-  const int k = segments_per_checkpoint > 0 ? segments_per_checkpoint : 64;
-  const size_t n = (size_t)std::max<int64_t>(c->n, 1);
-  if (!c->adj_last) {
-    ST_CUDA(cudaMalloc(&c->adj_last, 8 * n));
-    ST_CUDA(cudaMalloc(&c->adj_nseg, 8 * n));
-    ST_CUDA(cudaMalloc(&c->adj_head, sizeof(unsigned long long)));
-    ST_CUDA(cudaMalloc(&c->adj_overflow, sizeof(int)));
+  ST_TRY(adj_alloc_particle_arrays(c));
+  const int w_run = std::min(w_end, nwin_max);
+  size_t free_b = 0, total_b = 0;
+  ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  // checkpoints: slot 0 holds the start state, slot k the state at window k * every
+  int every = windows_per_checkpoint;
+  if (every == 0) {
+    const double budget = std::max(0.10 * (double)free_b, (double)c->arena_bytes);
+    every = (int)std::ceil((double)std::max(w_run, 1) * (double)c->arena_bytes / budget);
+    every = std::max(every, 1);
   }
-  size_t want = pool_bytes;
+  const int count = std::max(1, (w_run + every - 1) / every);
+  if (count > c->ckpt_alloc) {
+    cudaFree(c->ckpt_arena);
+    c->ckpt_arena = nullptr;
+    c->ckpt_alloc = 0;
+    cudaError_t e = cudaMalloc(&c->ckpt_arena, (size_t)count * c->arena_bytes);
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint checkpoints: ") + cudaGetErrorString(e));
+    c->ckpt_alloc = count;
+  }
+  if (!c->replay_arena) {
+    cudaError_t e = cudaMalloc(&c->replay_arena, c->arena_bytes);
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint replay state: ") + cudaGetErrorString(e));
+  }
+  c->ckpt_every = every;
+  c->ckpt_count = count;
+  // tape pool
+  size_t want = tape_bytes;
   if (want == 0) {
-    size_t free_b = 0, total_b = 0;
     ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    want = free_b / 4;
+    const double cap = 0.45 * (double)free_b;
+    const double guess = (double)std::max<int64_t>(c->n, 1) * 16.0 * 1048576.0 + 64.0 * 1048576.0;
+    want = (size_t)std::min(cap, guess);
   }
-  const int64_t cap = (int64_t)(want / st::adj_ckpt_bytes());
-  if (cap < 1) return fail(ST_ERR_ARG, "checkpoint pool too small");
-  if (cap != c->adj_pool_cap) {
-    cudaFree(c->adj_pool);
-    c->adj_pool = nullptr;
-    cudaError_t e = cudaMalloc(&c->adj_pool, (size_t)cap * st::adj_ckpt_bytes());
-    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("checkpoint pool: ") + cudaGetErrorString(e));
-    c->adj_pool_cap = cap;
+  const int64_t pages = std::min<int64_t>((int64_t)(want / kPageBytes), INT32_MAX - 1);
+  if (pages < 1) return fail(ST_ERR_ARG, "tape pool smaller than one page");
+  if (pages != c->tape_pages) {
+    cudaFree(c->tape_pool);
+    cudaFree(c->tape_prev);
+    c->tape_pool = nullptr;
+    c->tape_prev = nullptr;
+    c->tape_pages = 0;
+    cudaError_t e = cudaMalloc(&c->tape_pool, (size_t)pages * kPageBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->tape_prev, (size_t)pages * sizeof(int32_t));
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint tape pool: ") + cudaGetErrorString(e));
+    c->tape_pages = pages;
   }
+  // checkpoint 0 = the start state; later slots read "nothing to run" until written
+  ST_CUDA(cudaMemcpyAsync(c->ckpt_arena, c->arena, c->arena_bytes, cudaMemcpyDeviceToDevice, c->stream));
+  for (int k = 1; k < count; ++k) {
+    const st::DeviceState v = adj_view(c, (char*)c->ckpt_arena + (size_t)k * c->arena_bytes);
+    ST_CUDA(cudaMemsetAsync(v.w_done, 0x7f, 4 * (size_t)std::max<int64_t>(c->n, 1), c->stream));
+  }
+  ST_TRY(adj_reset_tape(c));
   ST_TRY(begin_run(c));
-  ST_CUDA(cudaMemsetAsync(c->adj_head, 0, sizeof(unsigned long long), c->stream));
-  ST_CUDA(cudaMemsetAsync(c->adj_overflow, 0, sizeof(int), c->stream));
   st::RunArgs a = make_args(c, 0, w_end, nullptr);
-  st::AdjArgs b{};
-  b.pool = (st::Ckpt*)c->adj_pool;
-  b.pool_head = c->adj_head;
-  b.pool_cap = c->adj_pool_cap;
-  b.last_ckpt = c->adj_last;
-  b.nseg = c->adj_nseg;
-  b.k = k;
-  b.overflow = c->adj_overflow;
-  int e = st::launch_adj_record(a, b, c->sm_count * 8, c->stream);
-  if (e) return fail(ST_ERR_CUDA, std::string("adjoint record launch: ") + cudaGetErrorString((cudaError_t)e));
-  int over = 0;
-  ST_CUDA(cudaMemcpyAsync(&over, c->adj_overflow, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  const st::TapeArgs t = adj_tape_args(c);
+  ST_TRY(adj_tape_launch(c, a, t));
+  const size_t n = (size_t)c->n;
+  c->adj_nsteps_h.assign(std::max<size_t>(n, 1), 0);
+  c->adj_nsegs_h.assign(std::max<size_t>(n, 1), 0);
+  c->adj_stop_h.assign(std::max<size_t>(n, 1), 0);
+  std::vector<int32_t> comp(std::max<size_t>(n, 1));
+  ST_CUDA(cudaMemcpyAsync(c->adj_nsteps_h.data(), t.nsteps, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaMemcpyAsync(c->adj_nsegs_h.data(), t.nsegs, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaMemcpyAsync(c->adj_stop_h.data(), c->s.stop, n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaMemcpyAsync(comp.data(), t.complete, 4 * n, cudaMemcpyDeviceToHost, c->stream));
   ST_TRY(end_run(c, 1));
   c->fresh = false;
   c->window_grid = true;
-  if (over) return fail(ST_ERR_NOMEM, "checkpoint pool exhausted: raise pool_bytes or segments_per_checkpoint");
-  c->adj_k = k;
+  bool resident = true;
+  uint64_t used = 0;
+  for (size_t i = 0; i < n; ++i) {
+    used += (uint64_t)tape_pages_for(c->adj_nsteps_h[i], c->adj_nsegs_h[i]) * kPageBytes;
+    if (!c->adj_stop_h[i] && !comp[i]) resident = false;
+  }
+  std::vector<int64_t> all(n);
+  for (size_t i = 0; i < n; ++i) all[i] = (int64_t)i;
+  ST_TRY(adj_upload_order(c, all, c->adj_order));
   c->adj_w_end = w_end;
+  c->adj_w_run = w_run;
+  c->adj_resident = resident;
   c->adj_recorded = true;
+  c->adj_stats = st_adjoint_stats{};
+  c->adj_stats.tape_bytes_used = used;
+  c->adj_stats.tape_bytes_pool = (uint64_t)c->tape_pages * kPageBytes;
+  c->adj_stats.resident = resident ? 1 : 0;
+  c->adj_stats.checkpoints = count;
+  c->adj_stats.windows_per_checkpoint = every;
   return ST_OK;
 }
 
@@ -809,42 +1070,46 @@ int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags)
   if (!c || !dL_dS || !grad) return fail(ST_ERR_ARG, "null argument");
   if (!c->adj_recorded) return fail(ST_ERR_STATE, "st_adjoint_backward needs st_adjoint_record first");
   ST_CUDA(cudaSetDevice(c->device));
-  const int blocks = c->sm_count * 2;
-  const int64_t lanes = (int64_t)blocks * 128;
-  const int step_cap = 1024;
-  if (!c->adj_segbuf || c->adj_lanes_blocks != blocks || c->adj_step_cap != step_cap || c->adj_seg_k != c->adj_k) {
-    cudaFree(c->adj_segbuf);
-    cudaFree(c->adj_stepbuf);
-    c->adj_segbuf = c->adj_stepbuf = nullptr;
-    cudaError_t e = cudaMalloc(&c->adj_segbuf, sizeof(double) * (size_t)lanes * (size_t)c->adj_k * st::kAdjSegF);
-    if (e == cudaSuccess) e = cudaMalloc(&c->adj_stepbuf, sizeof(double) * (size_t)lanes * (size_t)step_cap * 5);
-    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
-    c->adj_lanes_blocks = blocks;
-    c->adj_step_cap = step_cap;
-    c->adj_seg_k = c->adj_k;
+  const size_t n = (size_t)c->n;
+  c->adj_stats.replays = 0;
+  c->adj_stats.groups = 0;
+  if (n == 0) return ST_OK;
+  st::TapeArgs t = adj_tape_args(c);
+  t.grad = grad;
+  t.final_stop = c->s.stop;
+  t.pulse_grads = (flags & 1) ? 1 : 0;
+  ST_CUDA(cudaMemcpyAsync(t.lam, dL_dS, 24 * n, cudaMemcpyDeviceToDevice, c->stream));
+  ST_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * st::kNumTheta * n, c->stream));
+  ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(int), c->stream));
+  if (c->adj_resident) {
+    st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
+    a.order = c->adj_order;
+    a.nitems = c->n;
+    return adj_backward_launch(c, a, t);
   }
-  ST_TRY(begin_run(c));
-  st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
-  st::AdjArgs b{};
-  b.pool = (st::Ckpt*)c->adj_pool;
-  b.pool_cap = c->adj_pool_cap;
-  b.last_ckpt = c->adj_last;
-  b.nseg = c->adj_nseg;
-  b.k = c->adj_k;
-  b.dLdS = dL_dS;
-  b.grad = grad;
-  b.segbuf = c->adj_segbuf;
-  b.stepbuf = c->adj_stepbuf;
-  b.step_cap = step_cap;
-  b.pulse_grads = (flags & 1) ? 1 : 0;
-  b.overflow = c->adj_overflow;
-  ST_CUDA(cudaMemsetAsync(c->adj_overflow, 0, sizeof(int), c->stream));
-  int e = st::launch_adj_backward(a, b, blocks, c->stream);
-  if (e) return fail(ST_ERR_CUDA, std::string("adjoint backward launch: ") + cudaGetErrorString((cudaError_t)e));
-  int bad = 0;
-  ST_CUDA(cudaMemcpyAsync(&bad, c->adj_overflow, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  ST_TRY(end_run(c, 1));
-  if (bad) return fail(ST_ERR_CUDA, "internal: an adjoint block was larger than its scratch (skipped)");
+  // replay chunks of checkpoint intervals, last first, each sized from the
+  // record pass's tape length (time-uniform estimate; halves when it misses)
+  int64_t total_pages = 0, live = 0;
+  for (size_t i = 0; i < n; ++i) {
+    if (c->adj_stop_h[i]) continue;
+    total_pages += tape_pages_for(c->adj_nsteps_h[i], c->adj_nsegs_h[i]);
+    ++live;
+  }
+  const double per_interval = (double)total_pages / (double)c->ckpt_count + 2.0 * (double)live;
+  int k_hi = c->ckpt_count;
+  while (k_hi > 0) {
+    int span = (int)std::floor(0.85 * (double)c->tape_pages / std::max(per_interval, 1.0));
+    span = std::max(1, std::min(span, k_hi));
+    ST_TRY(adj_chunk(c, k_hi - span, k_hi, t));
+    k_hi -= span;
+  }
+  c->adj_resident = false;  // the pool now holds a replay's tape
+  return ST_OK;
+}
+
+int st_adjoint_get_stats(const st_ctx* c, st_adjoint_stats* out) {
+  if (!c || !out) return fail(ST_ERR_ARG, "null argument");
+  *out = c->adj_stats;
   return ST_OK;
 }
 

@@ -85,6 +85,7 @@ struct RunArgs {
   const SetParams* sets;
   int nsets;
   const int64_t* order;           // work order (persistent kernel), may be null
+  int64_t nitems;                 // items of the work queue (entries of order, else particles)
   DeviceState s;
   RunStatus* status;
   char* snap;                     // snapshot buffer base (device), may be null
@@ -97,26 +98,44 @@ struct RunArgs {
 // Discrete adjoint (st_adjoint.cu): gradient of L(S_final) with respect to
 // theta = [Gx(3), Gy(3), Gz(3), B0(3), E(3), a, w].
 constexpr int kNumTheta = 17;
-struct Ckpt;
-struct AdjArgs {
-  Ckpt* pool;                     // checkpoint pool
-  unsigned long long* pool_head;  // bump allocator cursor
-  int64_t pool_cap;
-  int64_t* last_ckpt;             // per particle: its last checkpoint (-1: none)
-  int64_t* nseg;                  // per particle: segments of the record pass
-  int k;                          // segments per checkpoint
-  const double* dLdS;             // per particle, 3 doubles
-  double* grad;                   // per particle, kNumTheta doubles
-  double* segbuf;                 // per lane: k segment records
-  double* stepbuf;                // per lane: step_cap records (y, x, h)
-  int step_cap;
+
+// The adjoint's tape, written by the trajectory-ahead kernel (k_batched with
+// its tape switch on): pages of kTapePageD doubles from one pool.  Every
+// particle owns two chains of pages, linked last to first: its accepted
+// DOP853 steps (y, x, h; h negated on the first step of a segment) and its
+// integrated segments (t0, p0, v0).
+constexpr int kTapePageD = 320;
+constexpr int kTapeStepD = 5, kTapeStepsPerPage = 64;
+constexpr int kTapeSegD = 8, kTapeSegsPerPage = 40;
+struct TapeArgs {
+  double* pool;
+  int32_t* page_prev;             // per page: the chain's previous page (-1: none)
+  unsigned long long* pool_head;  // page bump allocator (may run past pool_pages)
+  int64_t pool_pages;
+  // per particle
+  int32_t *step_page, *step_fill; // last page of the step chain and its records
+  int32_t *seg_page, *seg_fill;   // last page of the segment chain and its records
+  int64_t *nsteps, *nsegs;        // records of each chain, counted even when not stored
+  int32_t* complete;              // 1: both chains stored in full
+  // state checkpoints written at window ends (record pass): state k is the
+  // state after window k * ckpt_every - 1, at ckpt.<field> + k * ckpt_stride bytes
+  DeviceState ckpt;
+  int64_t ckpt_stride;
+  int ckpt_every, ckpt_count;
+  // backward pass
+  double* lam;                    // per particle: dL/dS at the end of the taped span (in, out)
+  double* grad;                   // per particle: kNumTheta accumulators (+=)
+  const uint8_t* final_stop;      // per particle: stopped at the end of the forward run
   int pulse_grads;
-  int* overflow;                  // set when the pool ran out
+  int* error;                     // set by a kernel that found an inconsistent tape
 };
-int launch_adj_record(const RunArgs& a, const AdjArgs& b, int blocks, void* stream);
-int launch_adj_backward(const RunArgs& a, const AdjArgs& b, int blocks, void* stream);
-size_t adj_ckpt_bytes();
-constexpr int kAdjSegF = 20;      // doubles per segment record of the backward pass
+// The trajectory-ahead kernel with its tape switch on (st_kernels.cu).
+int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);
+int tape_record_block();
+int tape_record_max_blocks_per_sm();
+int launch_adj_backward(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);
+int adj_backward_block();
+int adj_backward_max_blocks_per_sm();
 
 // Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
 // cast to int (0 = success).

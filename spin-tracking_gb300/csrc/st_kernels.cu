@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent(RunArgs a) {
     while (mode != M_SEG && mode != M_DONE) {
       if (mode == M_FETCH) {
         const unsigned long long item = atomicAdd(&a.status->queue_head, 1ull);
-        if (item >= (unsigned long long)a.s.n) {
+        if (item >= (unsigned long long)a.nitems) {
           mode = M_DONE;
           break;
         }
@@ -324,9 +324,87 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent(RunArgs a) {
 // collision, bits 8-15 sanity failure code.
 constexpr int kRecF = ST_GRAD_IS_LINEAR ? 8 : 14;
 
-template <int BLOCK>
+// ---- adjoint tape (TAPE instantiation only)
+// Cursor of one particle's two tape chains.
+struct TapeCursor {
+  int sp, sf, gp, gf;  // step chain: last page and its records; segment chain likewise
+  long long ns, ng;    // records counted (stored or not)
+  bool ok;             // every record so far was stored
+};
+
+__device__ __forceinline__ void tape_open(TapeCursor& c) {
+  c.sp = -1;
+  c.sf = kTapeStepsPerPage;
+  c.gp = -1;
+  c.gf = kTapeSegsPerPage;
+  c.ns = c.ng = 0;
+  c.ok = true;
+}
+
+// Address of a chain's next record, or null once the pool has run out (the
+// particle's tape is then incomplete and is rebuilt by a replay).
+__device__ __forceinline__ double* tape_slot(const TapeArgs& t, int& page, int& fill, int per_page, int rec_d,
+                                             bool& ok) {
+  if (!ok) return nullptr;
+  if (fill == per_page) {
+    const unsigned long long np = atomicAdd(t.pool_head, 1ull);
+    if (np >= (unsigned long long)t.pool_pages) {
+      ok = false;
+      return nullptr;
+    }
+    t.page_prev[np] = page;
+    page = (int)np;
+    fill = 0;
+  }
+  return t.pool + (size_t)page * kTapePageD + (size_t)(fill++) * rec_d;
+}
+
+__device__ __forceinline__ void tape_step(const TapeArgs& t, TapeCursor& c, double yx, double yy, double yz, double x,
+                                          double hs) {
+  ++c.ns;
+  double* r = tape_slot(t, c.sp, c.sf, kTapeStepsPerPage, kTapeStepD, c.ok);
+  if (r) {
+    r[0] = yx; r[1] = yy; r[2] = yz; r[3] = x; r[4] = hs;
+  }
+}
+
+__device__ __forceinline__ void tape_seg(const TapeArgs& t, TapeCursor& c, const SegStart& s0) {
+  ++c.ng;
+  double* r = tape_slot(t, c.gp, c.gf, kTapeSegsPerPage, kTapeSegD, c.ok);
+  if (r) {
+    r[0] = s0.t;
+    r[1] = s0.px; r[2] = s0.py; r[3] = s0.pz;
+    r[4] = s0.vx; r[5] = s0.vy; r[6] = s0.vz;
+    r[7] = 0.0;
+  }
+}
+
+__device__ __forceinline__ void tape_close(const TapeArgs& t, const TapeCursor& c, int64_t i) {
+  t.step_page[i] = c.sp;
+  t.step_fill[i] = c.sp < 0 ? 0 : c.sf;
+  t.seg_page[i] = c.gp;
+  t.seg_fill[i] = c.gp < 0 ? 0 : c.gf;
+  t.nsteps[i] = c.ns;
+  t.nsegs[i] = c.ng;
+  t.complete[i] = c.ok ? 1 : 0;
+}
+
+// View of state checkpoint k (same field layout as checkpoint 0, k * stride
+// bytes on; the set indices are shared by every slot).
+__device__ __forceinline__ DeviceState state_slot(const DeviceState& b, int64_t stride, int k) {
+  DeviceState s = b;
+  const int64_t o = stride * (int64_t)k;
+#define ST_OFF(f) s.f = reinterpret_cast<decltype(s.f)>(reinterpret_cast<char*>(b.f) + o);
+  ST_OFF(t) ST_OFF(px) ST_OFF(py) ST_OFF(pz) ST_OFF(vx) ST_OFF(vy) ST_OFF(vz) ST_OFF(Sx) ST_OFF(Sy) ST_OFF(Sz)
+  ST_OFF(h) ST_OFF(next_gas) ST_OFF(rx) ST_OFF(ry) ST_OFF(rz) ST_OFF(rw) ST_OFF(rspare) ST_OFF(rhas) ST_OFF(fail)
+  ST_OFF(n_coll) ST_OFF(n_bounce) ST_OFF(n_steps) ST_OFF(stop) ST_OFF(coll) ST_OFF(wall) ST_OFF(w_done)
+#undef ST_OFF
+  return s;
+}
+
+template <int BLOCK, bool TAPE>
 __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, double tf, double* qd, int* qf,
-                                               int slot, int tid, bool& blocked) {
+                                               int slot, int tid, bool& blocked, const TapeArgs& ta, TapeCursor& tc) {
   SegStart s0;
   const uint64_t nb = tp.n_bounce, nc = tp.n_coll;
   const bool fin = traj_event(tp, P, tf, s0);
@@ -343,6 +421,8 @@ __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, d
     r[11 * BLOCK] = s0.vx; r[12 * BLOCK] = s0.vy; r[13 * BLOCK] = s0.vz;
 #endif
   }
+  // the segments the spin side integrates, in order (the tape is DOP853-only)
+  if (TAPE && !tp.stop && tp.fail == 0) tape_seg(ta, tc, s0);
   qf[slot * BLOCK + tid] = (fin ? 1 : 0) | (tp.stop ? 2 : 0) | (tp.n_bounce != nb ? 4 : 0) |
                            (tp.n_coll != nc ? 8 : 0) | ((tp.fail & 0xff) << 8);
   if (fin || tp.stop) blocked = true;
@@ -350,8 +430,10 @@ __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, d
 
 enum BatchedMode { B_FETCH = 0, B_NEED = 1, B_SEG = 2, B_WEND = 3, B_DONE = 4 };
 
-template <int BLOCK, int MINB, int QCAP>
-__global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_start, int topup_keep) {
+// TAPE: also write the adjoint tape (steps and segments of every particle)
+// and state checkpoints at every ta.ckpt_every-th window end.
+template <int BLOCK, int MINB, int QCAP, bool TAPE>
+__global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_start, int topup_keep, TapeArgs ta) {
   extern __shared__ double st_smem[];
   double* qd = st_smem;
   int* qf = reinterpret_cast<int*>(st_smem + (size_t)QCAP * kRecF * BLOCK);
@@ -372,6 +454,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
   bool hit = false;
   const unsigned long long dl = run_deadline(a);
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  TapeCursor tc;
+  bool seg_first = false;  // no step of the open segment accepted yet
+  tape_open(tc);
   while (true) {
     // ---- A: spin-side boundaries of this lane (pop records, window ends, fetch)
     bool starved = false;
@@ -379,7 +464,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
     for (int guard = 0; guard < 8; ++guard) {
       if (mode == B_FETCH) {
         const unsigned long long item = atomicAdd(&a.status->queue_head, 1ull);
-        if (item >= (unsigned long long)a.s.n) {
+        if (item >= (unsigned long long)a.nitems) {
           mode = B_DONE;
           break;
         }
@@ -387,7 +472,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
         P = &a.sets[a.s.set[i]];
         w = a.s.w_done[i];
         wlast = min(a.w_end, P->nwin);
-        if (w >= wlast) continue;
+        if (TAPE) tape_open(tc);
+        if (w >= wlast) {
+          if (TAPE) tape_close(ta, tc, i);
+          continue;
+        }
         tp = load_state(a.s, i);
         s_fail = tp.fail;
         s_stop = tp.stop;
@@ -434,6 +523,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
             dop_begin(g, *P, tp.Sx, tp.Sy, tp.Sz, tempH);
           else
             rk45_begin(g, tempH);
+          seg_first = true;
           mode = B_SEG;
           break;
         } else {  // trajectory only: the segment completes at once
@@ -451,6 +541,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
         ++w;
         store_state(a.s, i, out);  // every window end is a resumable checkpoint
         a.s.w_done[i] = w;
+        if (TAPE && ta.ckpt_every > 0 && w % ta.ckpt_every == 0 && w / ta.ckpt_every < ta.ckpt_count) {
+          const DeviceState ck = state_slot(ta.ckpt, ta.ckpt_stride, w / ta.ckpt_every);
+          store_state(ck, i, out);
+          ck.w_done[i] = w;
+        }
+        if (TAPE && w >= wlast) tape_close(ta, tc, i);
         if (w < wlast) {
           tf = ((double)w + 1.0) * P->ioutInt;
           tempH = tp.h;
@@ -473,7 +569,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
         if (prod) {
           int slot = qhead + qcount;
           if (slot >= QCAP) slot -= QCAP;
-          produce_record<BLOCK>(tp, *P, tf, qd, qf, slot, tid, blocked);
+          produce_record<BLOCK, TAPE>(tp, *P, tf, qd, qf, slot, tid, blocked, ta, tc);
           ++qcount;
           ++n_seg;
         }
@@ -498,8 +594,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
     if (mode == B_SEG) {
       int r;
       if (P->integrator == 0) {
+        const double y0x = tp.Sx, y0y = tp.Sy, y0z = tp.Sz, x0 = g.x;
         r = dop_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
         ++n_dop;
+        if (TAPE && g.acc) {
+          tape_step(ta, tc, y0x, y0y, y0z, x0, seg_first ? -g.hu : g.hu);
+          seg_first = false;
+        }
       } else {
         r = rk45_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
         ++n_rk;
@@ -646,9 +747,9 @@ static const void* variant_fn(int v) {
     case 3: return reinterpret_cast<const void*>(&k_persistent<64, 4>);
     case 4: return reinterpret_cast<const void*>(&k_persistent<256, 1>);
     case 5:
-    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6>);
-    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4>);
-    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8>);
+    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false>);
+    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false>);
+    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false>);
   }
 }
 
@@ -687,11 +788,46 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
   if (e != cudaSuccess) return (int)e;
   RunArgs args = a;
   int t0 = x.tstart, t1 = x.tkeep;
+  TapeArgs none{};
   void* params_flat[] = {&args};
-  void* params_ahead[] = {&args, &t0, &t1};
+  void* params_ahead[] = {&args, &t0, &t1, &none};
   e = cudaLaunchKernel(variant_fn(v), dim3(blocks), dim3(x.block), x.family == 0 ? params_flat : params_ahead,
                        variant_smem(v), (cudaStream_t)stream);
   return (int)e;
+}
+
+// The record pass of the adjoint: the trajectory-ahead kernel with its tape on
+// (one configuration: 128 lanes, 6-record rings, top-up at 24 / 16 lanes).
+constexpr int kTapeBlock = 128, kTapeQcap = 6;
+static const void* tape_fn() { return reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true>); }
+static size_t tape_smem() { return (size_t)kTapeQcap * kTapeBlock * (kRecF * sizeof(double) + sizeof(int)); }
+
+static cudaError_t tape_ensure_smem() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(tape_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tape_smem());
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+int tape_record_block() { return kTapeBlock; }
+
+int tape_record_max_blocks_per_sm() {
+  int nb = 0;
+  if (tape_ensure_smem() != cudaSuccess) return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tape_fn(), kTapeBlock, tape_smem());
+  return nb;
+}
+
+int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream) {
+  if (a.nitems == 0) return 0;
+  cudaError_t e = tape_ensure_smem();
+  if (e != cudaSuccess) return (int)e;
+  RunArgs args = a;
+  TapeArgs tape = t;
+  int t0 = 24, t1 = 16;
+  void* params[] = {&args, &t0, &t1, &tape};
+  return (int)cudaLaunchKernel(tape_fn(), dim3(blocks), dim3(kTapeBlock), params, tape_smem(), (cudaStream_t)stream);
 }
 
 }  // namespace st

@@ -160,6 +160,7 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
   a.sets = params;
   a.nsets = nsets;
   a.order = nullptr;
+  a.nitems = n;
   a.s = carve(state, n);
   a.status = status;
   a.snap = nullptr;

@@ -17,7 +17,7 @@ from typing import Iterable
 import numpy as np
 
 from . import build
-from ._capi import (KERNEL_PERSISTENT, KERNEL_PLAIN, ST_ERR_DEADLINE, Counters, DeviceSoA, LaunchConfig, Options,
+from ._capi import (KERNEL_PERSISTENT, KERNEL_PLAIN, ST_ERR_DEADLINE, AdjointStats, Counters, DeviceSoA, LaunchConfig, Options,
                     SpinTrackError, StateView, Vec3, check, load)
 from .formats import read_format_a, snapshot_dtype
 
@@ -160,9 +160,19 @@ class Particles:
         """Copy the spins into a dense device array (3 doubles per particle) at dst_ptr."""
         check(load().st_gather_spins(self._ctx, ctypes.c_void_p(dst_ptr)))
 
-    def adjoint_record(self, w_end: int, segments_per_checkpoint: int = 0, pool_bytes: int = 0) -> None:
-        """Forward pass with checkpoints for adjoint_backward (needs a fresh init_particles)."""
-        check(load().st_adjoint_record(self._ctx, int(w_end), int(segments_per_checkpoint), int(pool_bytes)))
+    def adjoint_record(self, w_end: int, tape_bytes: int = 0, windows_per_checkpoint: int = 0) -> None:
+        """Forward pass writing the adjoint's tape (needs a fresh init_particles).
+
+        tape_bytes: device pool for the tape (0: up to 45% of free memory);
+        windows_per_checkpoint: state checkpoints for replays when the tape
+        does not fit (0: automatic)."""
+        check(load().st_adjoint_record(self._ctx, int(w_end), int(tape_bytes), int(windows_per_checkpoint)))
+
+    def adjoint_stats(self) -> dict:
+        """Tape size, pool size, and the replays the last backward needed."""
+        s = AdjointStats()
+        check(load().st_adjoint_get_stats(self._ctx, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in AdjointStats._fields_ if k != "pad"}
 
     def adjoint_backward(self, dLdS_ptr: int, grad_ptr: int, pulse: bool = False) -> None:
         """dL/dS (device, 3 doubles per particle) -> dL/dtheta per particle (device, 17 doubles)."""

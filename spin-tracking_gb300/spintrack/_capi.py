@@ -53,6 +53,13 @@ class LaunchConfig(ctypes.Structure):
     _fields_ = [("block_threads", c_int), ("blocks_per_sm", c_int), ("variant", c_int)]
 
 
+class AdjointStats(ctypes.Structure):
+    """st_adjoint_stats."""
+    _fields_ = [("tape_bytes_used", c_uint64), ("tape_bytes_pool", c_uint64), ("resident", ctypes.c_int32),
+                ("checkpoints", ctypes.c_int32), ("windows_per_checkpoint", ctypes.c_int32),
+                ("replays", ctypes.c_int32), ("groups", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
 class Counters(ctypes.Structure):
     _fields_ = [("dop_attempts", c_uint64), ("rk45_attempts", c_uint64), ("segments", c_uint64),
                 ("kernel_launches", c_uint64)]
@@ -101,7 +108,8 @@ _SIGS = {
     "st_get_counters": (c_int, [c_void_p, POINTER(Counters)]),
     "st_main_analysis": (c_int, [POINTER(Options), c_char_p, c_int, c_int, POINTER(c_double)]),
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),
-    "st_adjoint_record": (c_int, [c_void_p, c_int, c_int, c_size_t]),
+    "st_adjoint_record": (c_int, [c_void_p, c_int, c_size_t, c_int]),
+    "st_adjoint_get_stats": (c_int, [c_void_p, POINTER(AdjointStats)]),
     "st_adjoint_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     "st_run_noalloc": (c_int, [POINTER(Options), c_int, c_void_p, POINTER(c_size_t), c_int, c_void_p]),
     "st_write_header": (c_int, [c_void_p, POINTER(Options)]),

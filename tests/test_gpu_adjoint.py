@@ -115,7 +115,7 @@ def test_record_pass_is_the_forward_map(gpu):
         p.init_particles()
         p.run_windows(0, nw, st.KERNEL_PERSISTENT)
         q.init_particles()
-        q.adjoint_record(nw, segments_per_checkpoint=16)
+        q.adjoint_record(nw)
         a, b = p.output_data(), q.output_data()
     for f in a:
         np.testing.assert_array_equal(a[f], b[f], err_msg=f)
@@ -151,23 +151,45 @@ def test_ensemble_losses_backpropagate(gpu):
     assert torch.all(torch.isfinite(g1))
 
 
-def test_backward_after_changing_checkpoint_spacing(gpu):
-    """Record passes with different segments-per-checkpoint on one context
-    (the backward scratch is resized); gradients agree across spacings."""
+def _grad_with_budget(p, nw, w, tape_bytes, every):
     import torch
-    opt = adj_options(n=16, tf=0.1)
+    p.init_particles()
+    p.adjoint_record(nw, tape_bytes=tape_bytes, windows_per_checkpoint=every)
+    out = torch.empty(p.n, NUM_THETA, dtype=torch.float64, device=w.device)
+    torch.cuda.synchronize()
+    p.adjoint_backward(w.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), p.adjoint_stats()
+
+
+def test_backward_is_independent_of_the_tape_budget(gpu):
+    """The same gradients whether the record pass's tape fits (no replay), or
+    window chunks are replayed from state checkpoints, or a single window is
+    replayed in particle groups; final states identical in every case."""
+    import torch
+    opt = adj_options(n=16, tf=0.2)
     nw = st.num_windows(opt)
+    assert nw == 4
     dev = torch.device("cuda", 0)
-    grads = []
+    w = torch.tensor(np.random.default_rng(2).normal(size=(16, 3)), dtype=torch.float64, device=dev)
     with st.Particles(opt) as p:
-        for k in (4, 64, 256):
-            p.init_particles()
-            p.adjoint_record(nw, segments_per_checkpoint=k)
-            w = torch.zeros(opt.numParticles, 3, dtype=torch.float64, device=dev)
-            w[:, 0] = 1.0
-            out = torch.empty(opt.numParticles, NUM_THETA, dtype=torch.float64, device=dev)
-            torch.cuda.synchronize()
+        g_res, s_res = _grad_with_budget(p, nw, w, 0, 1)
+        S_res = p.output_data()["S"]
+        assert s_res["resident"] == 1 and s_res["replays"] == 0 and s_res["checkpoints"] == 4
+        used = s_res["tape_bytes_used"]
+        g_chunk, s_chunk = _grad_with_budget(p, nw, w, used // 2, 1)
+        assert s_chunk["resident"] == 0 and s_chunk["replays"] >= 2 and s_chunk["groups"] == 0
+        np.testing.assert_array_equal(p.output_data()["S"], S_res)
+        g_grp, s_grp = _grad_with_budget(p, nw, w, used // 16, 1)
+        assert s_grp["groups"] >= 2
+        np.testing.assert_array_equal(p.output_data()["S"], S_res)
+        # a pool below one particle's tape over one checkpoint interval
+        p.init_particles()
+        p.adjoint_record(nw, tape_bytes=2 * 320 * 8, windows_per_checkpoint=4)
+        out = torch.empty(16, NUM_THETA, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        with pytest.raises(st.SpinTrackError):
             p.adjoint_backward(w.data_ptr(), out.data_ptr())
-            grads.append(out.sum(0).cpu().numpy())
-    for g in grads[1:]:
-        np.testing.assert_allclose(g, grads[0], rtol=1e-12, atol=0.0)
+    assert np.all(np.isfinite(g_res))
+    np.testing.assert_allclose(g_chunk, g_res, rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(g_grp, g_res, rtol=1e-12, atol=1e-300)
