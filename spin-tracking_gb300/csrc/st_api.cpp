@@ -290,6 +290,8 @@ st::RunArgs make_args(st_ctx* c, int w_begin, int w_end, void* snap) {
   a.w_end = w_end;
   a.deadline_armed = 0;
   a.count_work = 1;
+  a.any_gas = 0;
+  for (const auto& P : c->sets_h) a.any_gas |= P.gas ? 1 : 0;
   return a;
 }
 

@@ -233,10 +233,54 @@ struct SegStart {
   double t, px, py, pz, vx, vy, vz;
 };
 
+// A cosine-law diffuse reflection whose draws were taken but whose velocity
+// is not yet computed (traj_event<true>).
+struct DiffuseDefer {
+  double su, theta, speed;  // sqrt(u1), 2 pi u2, |v| at the wall
+  char wall;
+  bool pending;
+};
+
+// New velocity of a cosine-law diffuse reflection off wall w (src/particle.cpp:309-328).
+__device__ __forceinline__ void diffuse_velocity(PState& p, double su, double theta, double speed, char w) {
+  const double phi = acos(su);
+  const double cp = cos(phi), sp = sin(phi), ct = cos(theta), stt = sin(theta);
+  if (w == 'x') {
+    p.vx = xmul(xmul(xmul(-1.0, sgn1(p.vx)), speed), cp);
+    p.vy = xmul(xmul(-speed, sp), ct);
+    p.vz = xmul(xmul(speed, sp), stt);
+  } else if (w == 'y') {
+    p.vx = xmul(xmul(speed, sp), ct);
+    p.vy = xmul(xmul(xmul(-1.0, sgn1(p.vy)), speed), cp);
+    p.vz = xmul(xmul(speed, sp), stt);
+  } else {
+    p.vx = xmul(xmul(speed, sp), ct);
+    p.vy = xmul(xmul(speed, sp), stt);
+    p.vz = xmul(xmul(xmul(-1.0, sgn1(p.vz)), speed), cp);
+  }
+}
+
 // One trajectory event: calc_next_collision_time, update_position_and_velocity
 // and sanity_check (src/particle.cpp:121-444).  Returns `finished` (the window
 // end tf was reached).  Fills the segment start.
-__device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double tf, SegStart& s0) {
+//
+// DEFER: a diffuse reflection's draws are taken here (the RNG sequence is
+// unchanged) but its velocity is left to diffuse_velocity, called later by the
+// trajectory-ahead kernel for many lanes at once.  The sanity check then sees
+// the velocity before the reflection; that gives the same outcome: the
+// reflected velocity is |v| times sines and cosines that are finite and, for
+// the draws possible here, non-zero except cos(phi) at u1 = 0, so it is NaN
+// or infinite only when the velocity before it already was, which fails the
+// same check (NaN) or the position check before it (infinite).
+//
+// GAS = false: compiled for launches in which no parameter set has gas
+// collisions.  Their gas clock is DBL_MAX and never moves, so the gas
+// collision is never the next event: either the wall time is finite and
+// smaller, or it is infinite and the step ends at the maxPosStep / window
+// limit either way.
+template <bool DEFER = false, bool GAS = true>
+__device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double tf, SegStart& s0,
+                                           DiffuseDefer* dd = nullptr) {
   const double G = kGravity;
   const double hLx = P.Lx / 2.0, hLy = P.Ly / 2.0, hLz = P.Lz / 2.0;
   double dtx, dty, dtz;
@@ -247,25 +291,33 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
     dtx = xdiv(dx, p.vx);
     dtz = xdiv(dz, p.vz);
     const double y2 = xmul(p.vy, p.vy);
-    if (sgn1(p.vy) <= 0.0) {  // moving down: the floor
+    // Moving down meets the floor; moving up meets the ceiling unless the apex
+    // is below it (then rise and fall to the floor).  Floor and ceiling share
+    // one root pair: the reference's ceiling roots (-vy + sq)/G, (-vy - sq)/G
+    // are bit for bit its floor roots (sq - vy)/G, -(sq + vy)/G in swapped
+    // order (IEEE addition commutes, negation is exact), and min(|r1|, |r2|)
+    // does not depend on the order (both roots are NaN together), so both
+    // branches run the same sqrt and divisions, once.
+    bool apex = false;
+    double arg = 0.0;
+    if (sgn1(p.vy) <= 0.0) {
       const double dy = xadd(p.py, xmul(P.Ly, 0.5));
-      const double sq = xsqrt(xadd(xmul(-2.0 * G, dy), y2));
+      arg = xadd(xmul(-2.0 * G, dy), y2);
+    } else {
+      const double top = xadd(xdiv(xmul(-0.5, y2), G), p.py);
+      apex = top < xmul(0.5, P.Ly);
+      arg = xsub(y2, xmul(2.0 * G, xsub(p.py, xmul(0.5, P.Ly))));
+    }
+    if (!apex) {
+      const double sq = xsqrt(arg);
       const double r1 = xdiv(-xadd(sq, p.vy), G);
       const double r2 = xdiv(xsub(sq, p.vy), G);
       dty = std_min(fabs(r1), fabs(r2));
     } else {
-      const double top = xadd(xdiv(xmul(-0.5, y2), G), p.py);
-      if (top < xmul(0.5, P.Ly)) {  // apex below the ceiling: rise, then fall to the floor
-        const double t1 = xdiv(-p.vy, G);
-        const double apex = xadd(xadd(p.py, xmul(p.vy, t1)), xmul(xmul(0.5 * G, t1), t1));
-        const double t2 = xsqrt(xdiv(xmul(xsub(xmul(-0.5, P.Ly), apex), 2.0), G));
-        dty = xadd(t1, t2);
-      } else {  // reaches the ceiling
-        const double sq = xsqrt(xsub(y2, xmul(2.0 * G, xsub(p.py, xmul(0.5, P.Ly)))));
-        const double r1 = xdiv(xadd(-p.vy, sq), G);
-        const double r2 = xdiv(xsub(-p.vy, sq), G);
-        dty = std_min(fabs(r1), fabs(r2));
-      }
+      const double t1 = xdiv(-p.vy, G);
+      const double ap = xadd(xadd(p.py, xmul(p.vy, t1)), xmul(xmul(0.5 * G, t1), t1));
+      const double t2 = xsqrt(xdiv(xmul(xsub(xmul(-0.5, P.Ly), ap), 2.0), G));
+      dty = xadd(t1, t2);
     }
     if (dtx < 1e-16 || isnan(dtx))  // only the first offending axis is replaced
       dtx = 1e6;
@@ -301,10 +353,12 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
     tb = dty; p.wall = 'd';  // y-z edge
   }
   // ---- gas collision, wall, window end or maxPosStep
-  const double to_gas = xsub(p.next_gas, p.t);
-  bool gas_next;
-  double to_col;
-  if (to_gas < tb) {
+  bool gas_next = false;
+  double to_col = tb;
+  const double to_gas = GAS ? xsub(p.next_gas, p.t) : 0.0;
+  if (!GAS) {
+    // no gas collisions in this launch
+  } else if (to_gas < tb) {
     gas_next = true;
     to_col = to_gas;
   } else if (to_gas == tb) {  // tie: the wall wins and the gas clock is redrawn
@@ -362,22 +416,20 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
     bool diffuse = false;
     if (P.diffuse > (double)FLT_MIN) diffuse = rng_uniform(p.rng) < P.diffuse;
     if (diffuse) {
-      // cosine-law diffuse reflection (src/particle.cpp:309-328)
-      const double phi = acos(xsqrt(rng_uniform(p.rng)));
+      // cosine-law diffuse reflection (src/particle.cpp:309-328): both draws
+      // now, the trigonometry now or (DEFER) batched later
+      const double su = xsqrt(rng_uniform(p.rng));
       const double theta = xmul(xmul(rng_uniform(p.rng), 2.0), 3.141592653589793);
-      const double cp = cos(phi), sp = sin(phi), ct = cos(theta), stt = sin(theta);
-      if (w == 'x') {
-        p.vx = xmul(xmul(xmul(-1.0, sgn1(p.vx)), speed), cp);
-        p.vy = xmul(xmul(-speed, sp), ct);
-        p.vz = xmul(xmul(speed, sp), stt);
-      } else if (w == 'y') {
-        p.vx = xmul(xmul(speed, sp), ct);
-        p.vy = xmul(xmul(xmul(-1.0, sgn1(p.vy)), speed), cp);
-        p.vz = xmul(xmul(speed, sp), stt);
-      } else if (w == 'z') {
-        p.vx = xmul(xmul(speed, sp), ct);
-        p.vy = xmul(xmul(speed, sp), stt);
-        p.vz = xmul(xmul(xmul(-1.0, sgn1(p.vz)), speed), cp);
+      if (w == 'x' || w == 'y' || w == 'z') {
+        if (DEFER) {
+          dd->su = su;
+          dd->theta = theta;
+          dd->speed = speed;
+          dd->wall = w;
+          dd->pending = true;
+        } else {
+          diffuse_velocity(p, su, theta, speed, w);
+        }
       } else {
         p.stop = true;  // a diffuse hit on an edge or corner stops the particle
       }
@@ -386,7 +438,7 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
       if (sy) p.vy = -p.vy;
       if (sz) p.vz = -p.vz;
     }
-  } else if (p.coll == 'G') {
+  } else if (GAS && p.coll == 'G') {
     if (P.dist == 'M') {
       p.vx = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);
       p.vy = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);

@@ -93,6 +93,7 @@ struct RunArgs {
   int w_begin, w_end;             // window range of this call
   int deadline_armed;             // read RunStatus::deadline_ns at kernel start
   int count_work;                 // accumulate attempt counters
+  int any_gas;                    // some set has gas collisions (else gas-free kernels may run)
 };
 
 // Discrete adjoint (st_adjoint.cu): gradient of L(S_final) with respect to

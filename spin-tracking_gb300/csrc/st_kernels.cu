@@ -402,12 +402,13 @@ __device__ __forceinline__ DeviceState state_slot(const DeviceState& b, int64_t 
   return s;
 }
 
-template <int BLOCK, bool TAPE>
+template <int BLOCK, bool TAPE, bool GAS>
 __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, double tf, double* qd, int* qf,
-                                               int slot, int tid, bool& blocked, const TapeArgs& ta, TapeCursor& tc) {
+                                               int slot, int tid, bool& blocked, DiffuseDefer& dd, const TapeArgs& ta,
+                                               TapeCursor& tc) {
   SegStart s0;
   const uint64_t nb = tp.n_bounce, nc = tp.n_coll;
-  const bool fin = traj_event(tp, P, tf, s0);
+  const bool fin = traj_event<true, GAS>(tp, P, tf, s0, &dd);
   double* r = qd + (size_t)slot * kRecF * BLOCK + tid;
   r[0 * BLOCK] = s0.t;
   r[1 * BLOCK] = tp.t;
@@ -430,10 +431,16 @@ __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, d
 
 enum BatchedMode { B_FETCH = 0, B_NEED = 1, B_SEG = 2, B_WEND = 3, B_DONE = 4 };
 
+// Diffuse reflections are deferred (traj_event<true>): a lane with one pending
+// produces no further records until the warp computes the pending
+// reflections together, when defer_k lanes have one, or one of them is about
+// to run dry or has reached its window end.
 // TAPE: also write the adjoint tape (steps and segments of every particle)
 // and state checkpoints at every ta.ckpt_every-th window end.
-template <int BLOCK, int MINB, int QCAP, bool TAPE>
-__global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_start, int topup_keep, TapeArgs ta) {
+// GAS = false: the instantiation for launches without gas collisions.
+template <int BLOCK, int MINB, int QCAP, bool TAPE, bool GAS>
+__global__ void __launch_bounds__(BLOCK, MINB)
+    k_batched(RunArgs a, int topup_start, int topup_keep, int defer_k, TapeArgs ta) {
   extern __shared__ double st_smem[];
   double* qd = st_smem;
   int* qf = reinterpret_cast<int*>(st_smem + (size_t)QCAP * kRecF * BLOCK);
@@ -457,6 +464,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
   TapeCursor tc;
   bool seg_first = false;  // no step of the open segment accepted yet
   tape_open(tc);
+  DiffuseDefer dd;
+  dd.pending = false;
   while (true) {
     // ---- A: spin-side boundaries of this lane (pop records, window ends, fetch)
     bool starved = false;
@@ -473,6 +482,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
         w = a.s.w_done[i];
         wlast = min(a.w_end, P->nwin);
         if (TAPE) tape_open(tc);
+        dd.pending = false;
         if (w >= wlast) {
           if (TAPE) tape_close(ta, tc, i);
           continue;
@@ -531,6 +541,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
           if (cur_fin) mode = B_WEND;
         }
       } else if (mode == B_WEND) {
+        // the window's last event reflected diffusely: its velocity is part of
+        // the state, computed in phase B first (one copy of that code)
+        if (dd.pending) break;
         PState out = tp;
         out.n_coll = s_ncoll;
         out.n_bounce = s_nbounce;
@@ -561,7 +574,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
     }
     // ---- B: warp-synchronous trajectory top-up
     const unsigned starved_m = __ballot_sync(FULL, starved);
-    bool prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP;
+    const unsigned defer_m = __ballot_sync(FULL, dd.pending);
+    if (defer_m != 0u &&
+        (__popc(defer_m) >= defer_k || __any_sync(FULL, dd.pending && (starved || qcount <= 1 || mode == B_WEND)))) {
+      if (dd.pending) {
+        diffuse_velocity(tp, dd.su, dd.theta, dd.speed, dd.wall);
+        dd.pending = false;
+      }
+    }
+    bool prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP && !dd.pending;
     unsigned pm = __ballot_sync(FULL, prod);
     if (starved_m != 0u || __popc(pm) >= topup_start) {
 #pragma unroll 1
@@ -569,11 +590,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_batched(RunArgs a, int topup_st
         if (prod) {
           int slot = qhead + qcount;
           if (slot >= QCAP) slot -= QCAP;
-          produce_record<BLOCK, TAPE>(tp, *P, tf, qd, qf, slot, tid, blocked, ta, tc);
+          produce_record<BLOCK, TAPE, GAS>(tp, *P, tf, qd, qf, slot, tid, blocked, dd, ta, tc);
           ++qcount;
           ++n_seg;
         }
-        prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP;
+        prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP && !dd.pending;
         pm = __ballot_sync(FULL, prod);
         if (pm == 0u || __popc(pm) < topup_keep) break;
       }
@@ -724,22 +745,24 @@ int launch_pack_snapshot(const RunArgs& a, int slot, void* stream) {
 // while this many still have room).  Block threads and the minimum resident
 // blocks per SM set the register budget.
 struct Variant {
-  int family, block, minb, qcap, tstart, tkeep;
+  int family, block, minb, qcap, tstart, tkeep, defer;
   const char* name;
 };
 static const Variant kVariants[] = {
-    {0, 128, 1, 0, 0, 0, "flat_b128_m1"},  {0, 128, 2, 0, 0, 0, "flat_b128_m2"},
-    {0, 128, 3, 0, 0, 0, "flat_b128_m3"},  {0, 64, 4, 0, 0, 0, "flat_b64_m4"},
-    {0, 256, 1, 0, 0, 0, "flat_b256_m1"},  {1, 128, 1, 6, 24, 16, "ahead_b128_q6_t24"},
-    {1, 128, 1, 6, 16, 12, "ahead_b128_q6_t16"}, {1, 128, 2, 4, 24, 16, "ahead_b128_q4_t24"},
-    {1, 64, 2, 8, 24, 16, "ahead_b64_q8_t24"},
+    {0, 128, 1, 0, 0, 0, 0, "flat_b128_m1"},  {0, 128, 2, 0, 0, 0, 0, "flat_b128_m2"},
+    {0, 128, 3, 0, 0, 0, 0, "flat_b128_m3"},  {0, 64, 4, 0, 0, 0, 0, "flat_b64_m4"},
+    {0, 256, 1, 0, 0, 0, 0, "flat_b256_m1"},  {1, 128, 1, 6, 24, 16, 12, "ahead_b128_q6_t24_d12"},
+    {1, 128, 1, 6, 16, 12, 12, "ahead_b128_q6_t16_d12"}, {1, 128, 2, 4, 24, 16, 12, "ahead_b128_q4_t24_d12"},
+    {1, 64, 2, 8, 24, 16, 12, "ahead_b64_q8_t24_d12"},   {1, 64, 2, 8, 24, 16, 6, "ahead_b64_q8_t24_d6"},
+    {1, 64, 2, 8, 24, 16, 18, "ahead_b64_q8_t24_d18"},   {1, 64, 2, 8, 28, 20, 12, "ahead_b64_q8_t28_d12"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int persistent_variant_count() { return kNumVariants; }
 const char* persistent_variant_name(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "?"; }
 
-static const void* variant_fn(int v) {
+template <bool GAS>
+static const void* variant_fn_g(int v) {
   switch (v) {
     case 0: return reinterpret_cast<const void*>(&k_persistent<128, 1>);
     case 1: return reinterpret_cast<const void*>(&k_persistent<128, 2>);
@@ -747,11 +770,12 @@ static const void* variant_fn(int v) {
     case 3: return reinterpret_cast<const void*>(&k_persistent<64, 4>);
     case 4: return reinterpret_cast<const void*>(&k_persistent<256, 1>);
     case 5:
-    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false>);
-    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false>);
-    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false>);
+    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, GAS>);
+    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, GAS>);
+    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS>);  // 8 and up
   }
 }
+static const void* variant_fn(int v, bool gas) { return gas ? variant_fn_g<true>(v) : variant_fn_g<false>(v); }
 
 static size_t variant_smem(int v) {
   const Variant& x = kVariants[v];
@@ -760,13 +784,13 @@ static size_t variant_smem(int v) {
 }
 
 // Opt the kernels that need more than 48 KiB of dynamic shared memory in, once.
-static cudaError_t ensure_smem(int v) {
-  static bool done[kNumVariants] = {};
-  if (done[v]) return cudaSuccess;
+static cudaError_t ensure_smem(int v, bool gas) {
+  static bool done[kNumVariants][2] = {};
+  if (done[v][gas]) return cudaSuccess;
   const size_t sm = variant_smem(v);
   cudaError_t e = cudaSuccess;
-  if (sm > 0) e = cudaFuncSetAttribute(variant_fn(v), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e == cudaSuccess) done[v] = true;
+  if (sm > 0) e = cudaFuncSetAttribute(variant_fn(v, gas), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess) done[v][gas] = true;
   return e;
 }
 
@@ -774,8 +798,9 @@ int persistent_max_blocks_per_sm(int v, int block) {
   int nb = 0;
   if (v < 0 || v >= kNumVariants) return 0;
   (void)block;
-  if (ensure_smem(v) != cudaSuccess) return 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, variant_fn(v), kVariants[v].block, variant_smem(v));
+  // both instantiations have the same launch bounds; take the one with gas
+  if (ensure_smem(v, true) != cudaSuccess) return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, variant_fn(v, true), kVariants[v].block, variant_smem(v));
   return nb;
 }
 
@@ -784,14 +809,15 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
   if (v < 0 || v >= kNumVariants) return (int)cudaErrorInvalidValue;
   (void)block;
   const Variant& x = kVariants[v];
-  cudaError_t e = ensure_smem(v);
+  const bool gas = a.any_gas != 0;
+  cudaError_t e = ensure_smem(v, gas);
   if (e != cudaSuccess) return (int)e;
   RunArgs args = a;
-  int t0 = x.tstart, t1 = x.tkeep;
+  int t0 = x.tstart, t1 = x.tkeep, dk = x.defer;
   TapeArgs none{};
   void* params_flat[] = {&args};
-  void* params_ahead[] = {&args, &t0, &t1, &none};
-  e = cudaLaunchKernel(variant_fn(v), dim3(blocks), dim3(x.block), x.family == 0 ? params_flat : params_ahead,
+  void* params_ahead[] = {&args, &t0, &t1, &dk, &none};
+  e = cudaLaunchKernel(variant_fn(v, gas), dim3(blocks), dim3(x.block), x.family == 0 ? params_flat : params_ahead,
                        variant_smem(v), (cudaStream_t)stream);
   return (int)e;
 }
@@ -799,14 +825,17 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
 // The record pass of the adjoint: the trajectory-ahead kernel with its tape on
 // (one configuration: 128 lanes, 6-record rings, top-up at 24 / 16 lanes).
 constexpr int kTapeBlock = 128, kTapeQcap = 6;
-static const void* tape_fn() { return reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true>); }
+static const void* tape_fn(bool gas) {
+  return gas ? reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, true>)
+             : reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, false>);
+}
 static size_t tape_smem() { return (size_t)kTapeQcap * kTapeBlock * (kRecF * sizeof(double) + sizeof(int)); }
 
-static cudaError_t tape_ensure_smem() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(tape_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tape_smem());
-  if (e == cudaSuccess) done = true;
+static cudaError_t tape_ensure_smem(bool gas) {
+  static bool done[2] = {};
+  if (done[gas]) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(tape_fn(gas), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tape_smem());
+  if (e == cudaSuccess) done[gas] = true;
   return e;
 }
 
@@ -814,20 +843,22 @@ int tape_record_block() { return kTapeBlock; }
 
 int tape_record_max_blocks_per_sm() {
   int nb = 0;
-  if (tape_ensure_smem() != cudaSuccess) return 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tape_fn(), kTapeBlock, tape_smem());
+  if (tape_ensure_smem(true) != cudaSuccess) return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tape_fn(true), kTapeBlock, tape_smem());
   return nb;
 }
 
 int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream) {
   if (a.nitems == 0) return 0;
-  cudaError_t e = tape_ensure_smem();
+  const bool gas = a.any_gas != 0;
+  cudaError_t e = tape_ensure_smem(gas);
   if (e != cudaSuccess) return (int)e;
   RunArgs args = a;
   TapeArgs tape = t;
-  int t0 = 24, t1 = 16;
-  void* params[] = {&args, &t0, &t1, &tape};
-  return (int)cudaLaunchKernel(tape_fn(), dim3(blocks), dim3(kTapeBlock), params, tape_smem(), (cudaStream_t)stream);
+  int t0 = 24, t1 = 16, dk = 12;
+  void* params[] = {&args, &t0, &t1, &dk, &tape};
+  return (int)cudaLaunchKernel(tape_fn(gas), dim3(blocks), dim3(kTapeBlock), params, tape_smem(),
+                               (cudaStream_t)stream);
 }
 
 }  // namespace st
