@@ -163,9 +163,14 @@ const char *st_launch_variant_name(int variant);
  * ST_ERR_DEADLINE; calling again resumes. */
 int st_set_deadline(st_ctx *ctx, double seconds);
 /* Work counters of the last run call: DOP853 and RK45 step attempts,
- * trajectory segments, and kernels launched. */
+ * trajectory segments, and kernels launched.  st_run_windows enqueues its
+ * launches as one CUDA graph, captured on the first call with a given
+ * (kernel, window range, snapshot buffer, launch configuration, deadline) and
+ * replayed by later calls: graph_launches = 1 for such a call, graph_captures
+ * = 1 when it captured a new graph. */
 typedef struct st_counters {
   uint64_t dop_attempts, rk45_attempts, segments, kernel_launches;
+  uint64_t graph_launches, graph_captures;
 } st_counters;
 int st_get_counters(const st_ctx *ctx, st_counters *out);
 
@@ -228,6 +233,35 @@ typedef struct {
   int32_t pad;
 } st_adjoint_stats;
 int st_adjoint_get_stats(const st_ctx *ctx, st_adjoint_stats *out);
+
+/* ---- ensemble statistics (on the device) ------------------------------ */
+/* The reference computes these in its analysis scripts from the output file
+ * (scripts/nedmSim.py:151-179 shiftDatapoints,
+ * benchmarks/CheckingFrequencyShiftFromEField.ipynb analyzeDataset); here
+ * they are reduced on the device, so a parameter sweep needs no file.  Over
+ * the particles of one set with failureState 0 and a finite phase
+ * phi = atan2(Sz, Sy): the phases are aligned to the most populated of 1000
+ * equal bins (numpy.histogram binning) and clipped at 5 standard deviations,
+ * as shiftDatapoints does; frequency shift = wrap(phase_mean - phase_expected)
+ * / (2 pi t) with phase_expected = atan2(cos(w t), sin(w t)),
+ * w = gamma |B0| sign(B0x).  phase_stderr = phase_std / sqrt(n_phase) (the
+ * notebook divides by the square root of the number of snapshots instead). */
+typedef struct {
+  double t;               /* time of the snapshot (first counted particle) */
+  int64_t n_valid;        /* particles counted */
+  int64_t n_phase;        /* of those, kept by the 5-sigma clip */
+  double mean_S[3];       /* mean spin of the counted particles */
+  double polarisation;    /* |mean_S| */
+  double phase_mean;      /* aligned, clipped mean phase, wrapped to [-pi, pi] */
+  double phase_std;       /* population standard deviation of the same phases */
+  double phase_stderr;    /* phase_std / sqrt(n_phase) */
+  double phase_expected;
+  double freq_shift;      /* Hz */
+  double freq_shift_err;  /* phase_stderr / (2 pi t), Hz */
+} st_ensemble;
+/* snap: a device snapshot block (st_snapshot_bytes) or NULL for the current
+ * state; set: parameter-set index. */
+int st_ensemble_stats(st_ctx *ctx, const void *snap, int set, st_ensemble *out);
 
 /* FP64 FMA issue-rate probe (TFLOP/s, FMA = 2 flops): eight independent
  * DFMA chains per thread on every SM.  No counterpart in the reference; it is

@@ -168,6 +168,16 @@ struct st_ctx {
   st::SnapLayout snap{};
   bool fresh = false;        // st_init ran and no run call since
   size_t arena_bytes = 0;    // bytes of one particle-state arena (state_layout)
+  // CUDA graphs of st_run_windows calls, most recent last
+  struct RunGraph {
+    int kernel, w_begin, w_end, block, variant, bps;
+    void* snap;
+    double deadline_s;
+    cudaGraphExec_t exec;
+    int launches;
+  };
+  std::vector<RunGraph> graphs;
+  void* ens_buf = nullptr;   // ensemble statistics: control slots, block partials, histogram
   // adjoint (allocated by st_adjoint_record)
   double* tape_pool = nullptr;
   int32_t* tape_prev = nullptr;
@@ -312,6 +322,8 @@ int end_run(st_ctx* c, int launches) {
   c->last.rk45_attempts = c->status_h->rk45_attempts;
   c->last.segments = c->status_h->segments;
   c->last.kernel_launches = (uint64_t)launches;
+  c->last.graph_launches = 0;
+  c->last.graph_captures = 0;
   if (c->status_h->pad) return fail(ST_ERR_CUDA, "internal: a persistent-kernel lane could not make progress");
   if (c->status_h->deadline_hit) return fail(ST_ERR_DEADLINE, "device time budget ran out; state saved at window ends");
   return ST_OK;
@@ -568,6 +580,8 @@ void st_destroy(st_ctx* c) {
   cudaFree(c->sets_d);
   cudaFree(c->status_d);
   cudaFree(c->order_d);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  cudaFree(c->ens_buf);
   cudaFree(c->tape_pool);
   cudaFree(c->tape_prev);
   cudaFree(c->tape_pp);
@@ -608,36 +622,89 @@ int st_run_until(st_ctx* c, double next_t) {
   return end_run(c, 1);
 }
 
-int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
-  if (!c) return fail(ST_ERR_ARG, "null context");
-  if (!c->initialized) return fail(ST_ERR_STATE, "st_run_windows before st_init");
-  if (!c->window_grid) return fail(ST_ERR_STATE, "particles were advanced off the window grid by st_run_until");
-  if (w_begin < 0 || w_end < w_begin) return fail(ST_ERR_ARG, "bad window range");
-  if (w_end == w_begin) return ST_OK;
-  ST_TRY(begin_run(c));
-  c->fresh = false;
-  c->adj_recorded = false;
-  int launches = 0;
+namespace {
+constexpr size_t kMaxRunGraphs = 8;
+
+// The launches of one st_run_windows call, enqueued on the context's stream.
+int enqueue_run(st_ctx* c, int kernel, int w_begin, int w_end, void* snap, int* launches) {
+  ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
   if (kernel == ST_KERNEL_PLAIN) {
     st::RunArgs a = make_args(c, w_begin, w_end, snap);
     ST_TRY(arm_deadline(c, a));
     for (int w = w_begin; w < w_end; ++w) {
       int e = st::launch_plain_window(a, w, plain_block(c), c->stream);
       if (e) return fail(ST_ERR_CUDA, std::string("plain launch: ") + cudaGetErrorString((cudaError_t)e));
-      ++launches;
+      ++*launches;
       if (snap) {
         e = st::launch_pack_snapshot(a, w - w_begin, c->stream);
         if (e) return fail(ST_ERR_CUDA, std::string("pack launch: ") + cudaGetErrorString((cudaError_t)e));
-        ++launches;
+        ++*launches;
       }
     }
-  } else if (kernel == ST_KERNEL_PERSISTENT) {
-    ST_TRY(run_persistent(c, w_begin, w_end, snap));
-    ++launches;
-  } else {
-    return fail(ST_ERR_ARG, "unknown kernel selector");
+    return ST_OK;
   }
-  return end_run(c, launches);
+  ST_TRY(run_persistent(c, w_begin, w_end, snap));
+  ++*launches;
+  return ST_OK;
+}
+}  // namespace
+
+int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
+  if (!c) return fail(ST_ERR_ARG, "null context");
+  if (!c->initialized) return fail(ST_ERR_STATE, "st_run_windows before st_init");
+  if (!c->window_grid) return fail(ST_ERR_STATE, "particles were advanced off the window grid by st_run_until");
+  if (w_begin < 0 || w_end < w_begin) return fail(ST_ERR_ARG, "bad window range");
+  if (kernel != ST_KERNEL_PLAIN && kernel != ST_KERNEL_PERSISTENT) return fail(ST_ERR_ARG, "unknown kernel selector");
+  if (w_end == w_begin) return ST_OK;
+  ST_CUDA(cudaSetDevice(c->device));
+  if (kernel == ST_KERNEL_PERSISTENT) {  // allocations and tuning happen outside the capture
+    ST_TRY(ctx_build_order(c));
+    if (c->lc.variant < 0 || c->lc.blocks_per_sm <= 0) ST_TRY(autotune(c));
+    if (int e = st::persistent_prepare(c->lc.variant))
+      return fail(ST_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString((cudaError_t)e));
+  }
+  c->fresh = false;
+  c->adj_recorded = false;
+  const int block = kernel == ST_KERNEL_PLAIN ? plain_block(c) : 0;
+  const int var = kernel == ST_KERNEL_PLAIN ? -1 : c->lc.variant;
+  const int bps = kernel == ST_KERNEL_PLAIN ? 0 : c->lc.blocks_per_sm;
+  size_t hit = c->graphs.size();
+  for (size_t k = 0; k < c->graphs.size(); ++k) {
+    const auto& g = c->graphs[k];
+    if (g.kernel == kernel && g.w_begin == w_begin && g.w_end == w_end && g.snap == snap && g.block == block &&
+        g.variant == var && g.bps == bps && g.deadline_s == c->deadline_s)
+      hit = k;
+  }
+  bool captured = false;
+  if (hit == c->graphs.size()) {
+    int launches = 0;
+    cudaGraph_t graph = nullptr;
+    ST_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_run(c, kernel, w_begin, w_end, snap, &launches);
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (rc != ST_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(ST_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return fail(ST_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    if (c->graphs.size() >= kMaxRunGraphs) {
+      cudaGraphExecDestroy(c->graphs.front().exec);
+      c->graphs.erase(c->graphs.begin());
+    }
+    c->graphs.push_back({kernel, w_begin, w_end, block, var, bps, snap, c->deadline_s, exec, launches});
+    hit = c->graphs.size() - 1;
+    captured = true;
+  }
+  const st_ctx::RunGraph g = c->graphs[hit];
+  ST_CUDA(cudaGraphLaunch(g.exec, c->stream));
+  const int rc = end_run(c, g.launches);
+  c->last.graph_launches = 1;
+  c->last.graph_captures = captured ? 1 : 0;
+  return rc;
 }
 
 size_t st_snapshot_bytes(const st_ctx* c) { return c ? c->snap.bytes : 0; }
@@ -1112,6 +1179,68 @@ int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags)
 int st_adjoint_get_stats(const st_ctx* c, st_adjoint_stats* out) {
   if (!c || !out) return fail(ST_ERR_ARG, "null argument");
   *out = c->adj_stats;
+  return ST_OK;
+}
+
+int st_ensemble_stats(st_ctx* c, const void* snap, int set, st_ensemble* out) {
+  if (!c || !out) return fail(ST_ERR_ARG, "null argument");
+  if (set < 0 || set >= (int)c->sets_h.size()) return fail(ST_ERR_ARG, "no such parameter set");
+  ST_CUDA(cudaSetDevice(c->device));
+  const size_t ctl_b = 256, part_b = sizeof(double) * 8 * st::kEnsMaxBlocks;
+  if (!c->ens_buf) {
+    cudaError_t e = cudaMalloc(&c->ens_buf, ctl_b + part_b + sizeof(unsigned int) * st::kEnsHistBins);
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("ensemble scratch: ") + cudaGetErrorString(e));
+  }
+  double* ctl = (double*)c->ens_buf;
+  double* part = (double*)((char*)c->ens_buf + ctl_b);
+  unsigned int* hist = (unsigned int*)((char*)c->ens_buf + ctl_b + part_b);
+  const double *t, *sx, *sy, *sz;
+  const int32_t* fl;
+  if (snap) {
+    const char* b = (const char*)snap;
+    t = (const double*)(b + c->snap.off[0]);
+    sx = (const double*)(b + c->snap.off[7]);
+    sy = (const double*)(b + c->snap.off[8]);
+    sz = (const double*)(b + c->snap.off[9]);
+    fl = (const int32_t*)(b + c->snap.off[10]);
+  } else {
+    t = c->s.t;
+    sx = c->s.Sx;
+    sy = c->s.Sy;
+    sz = c->s.Sz;
+    fl = c->s.fail;
+  }
+  const SetParams& P = c->sets_h[(size_t)set];
+  int e = st::ensemble_device(t, sx, sy, sz, fl, P.first, P.n, ctl, part, hist, st::kEnsMaxBlocks, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("ensemble launch: ") + cudaGetErrorString((cudaError_t)e));
+  double h[32];
+  ST_CUDA(cudaMemcpyAsync(h, ctl, sizeof(double) * st::ensemble_ctl_count(), cudaMemcpyDeviceToHost, c->stream));
+  cudaError_t se = cudaStreamSynchronize(c->stream);
+  if (se != cudaSuccess) return fail(ST_ERR_CUDA, std::string("ensemble: ") + cudaGetErrorString(se));
+  const double pi = 3.141592653589793;
+  const double n = h[st::ENS_COUNT];
+  st_ensemble r{};
+  r.t = h[st::ENS_T];
+  r.n_valid = (int64_t)n;
+  r.n_phase = (int64_t)h[st::ENS_KEPT];
+  for (int k = 0; k < 3; ++k) r.mean_S[k] = h[st::ENS_SX + k] / n;
+  r.polarisation = std::sqrt(r.mean_S[0] * r.mean_S[0] + r.mean_S[1] * r.mean_S[1] + r.mean_S[2] * r.mean_S[2]);
+  double m = h[st::ENS_MEAN2];
+  if (m > pi) m -= 2.0 * pi;
+  if (m < -pi) m += 2.0 * pi;
+  r.phase_mean = m;
+  r.phase_std = h[st::ENS_STD2];
+  r.phase_stderr = r.phase_std / std::sqrt(h[st::ENS_KEPT]);
+  const double b0 = std::sqrt(P.B0x * P.B0x + P.B0y * P.B0y + P.B0z * P.B0z);
+  const double sgn = P.B0x > 0.0 ? 1.0 : (P.B0x < 0.0 ? -1.0 : 0.0);
+  const double w = P.gamma * b0 * sgn;
+  r.phase_expected = std::atan2(std::cos(w * r.t), std::sin(w * r.t));
+  double shift = r.phase_mean - r.phase_expected;
+  if (shift > pi) shift -= 2.0 * pi;
+  if (shift < -pi) shift += 2.0 * pi;
+  r.freq_shift = shift / r.t / (2.0 * pi);
+  r.freq_shift_err = r.phase_stderr / r.t / (2.0 * pi);
+  *out = r;
   return ST_OK;
 }
 

@@ -138,6 +138,15 @@ int launch_adj_backward(const RunArgs& a, const TapeArgs& t, int blocks, void* s
 int adj_backward_block();
 int adj_backward_max_blocks_per_sm();
 
+// Ensemble statistics (st_ensemble.cu).
+int ensemble_device(const double* t, const double* Sx, const double* Sy, const double* Sz, const int32_t* fail,
+                    int64_t first, int64_t n, double* ctl, double* part, unsigned int* hist, int max_blocks,
+                    void* stream);
+int ensemble_ctl_count();
+constexpr int kEnsMaxBlocks = 1024, kEnsHistBins = 1000;
+enum { ENS_COUNT = 0, ENS_SX, ENS_SY, ENS_SZ, ENS_MIN, ENS_MAX, ENS_T, ENS_EDGE0, ENS_EDGE1, ENS_LOC, ENS_MEAN1,
+       ENS_STD1, ENS_MEAN2, ENS_STD2, ENS_KEPT };
+
 // Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
 // cast to int (0 = success).
 int launch_prepare_sets(SetParams* sets, int nsets, void* stream);
@@ -153,6 +162,7 @@ int persistent_variant_count();
 int build_set_params(const st_options& o, int64_t first, SetParams* P);
 int set_last_error(int code, const char* msg);
 int persistent_max_blocks_per_sm(int variant, int block);
+int persistent_prepare(int variant);
 const char* persistent_variant_name(int variant);
 
 }  // namespace st

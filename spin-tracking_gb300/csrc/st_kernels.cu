@@ -794,6 +794,14 @@ static cudaError_t ensure_smem(int v, bool gas) {
   return e;
 }
 
+// Function attributes of a variant's kernels, set before any graph capture.
+int persistent_prepare(int v) {
+  if (v < 0 || v >= kNumVariants) return (int)cudaErrorInvalidValue;
+  cudaError_t e = ensure_smem(v, true);
+  if (e == cudaSuccess) e = ensure_smem(v, false);
+  return (int)e;
+}
+
 int persistent_max_blocks_per_sm(int v, int block) {
   int nb = 0;
   if (v < 0 || v >= kNumVariants) return 0;

@@ -17,7 +17,7 @@ from typing import Iterable
 import numpy as np
 
 from . import build
-from ._capi import (KERNEL_PERSISTENT, KERNEL_PLAIN, ST_ERR_DEADLINE, AdjointStats, Counters, DeviceSoA, LaunchConfig, Options,
+from ._capi import (KERNEL_PERSISTENT, KERNEL_PLAIN, ST_ERR_DEADLINE, AdjointStats, Counters, Ensemble, DeviceSoA, LaunchConfig, Options,
                     SpinTrackError, StateView, Vec3, check, load)
 from .formats import read_format_a, snapshot_dtype
 
@@ -167,6 +167,16 @@ class Particles:
         windows_per_checkpoint: state checkpoints for replays when the tape
         does not fit (0: automatic)."""
         check(load().st_adjoint_record(self._ctx, int(w_end), int(tape_bytes), int(windows_per_checkpoint)))
+
+    def ensemble(self, set_index: int = 0, snap_ptr: int = 0) -> dict:
+        """Mean spin, polarisation, aligned/clipped precession phase and frequency
+        shift of one parameter set (st_ensemble_stats), from the current state or
+        from the device snapshot block at snap_ptr."""
+        e = Ensemble()
+        check(load().st_ensemble_stats(self._ctx, ctypes.c_void_p(snap_ptr or None), int(set_index), ctypes.byref(e)))
+        d = {k: getattr(e, k) for k, _ in Ensemble._fields_}
+        d["mean_S"] = tuple(e.mean_S)
+        return d
 
     def adjoint_stats(self) -> dict:
         """Tape size, pool size, and the replays the last backward needed."""

@@ -60,9 +60,17 @@ class AdjointStats(ctypes.Structure):
                 ("replays", ctypes.c_int32), ("groups", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
+class Ensemble(ctypes.Structure):
+    """st_ensemble."""
+    _fields_ = [("t", c_double), ("n_valid", c_int64), ("n_phase", c_int64), ("mean_S", c_double * 3),
+                ("polarisation", c_double), ("phase_mean", c_double), ("phase_std", c_double),
+                ("phase_stderr", c_double), ("phase_expected", c_double), ("freq_shift", c_double),
+                ("freq_shift_err", c_double)]
+
+
 class Counters(ctypes.Structure):
     _fields_ = [("dop_attempts", c_uint64), ("rk45_attempts", c_uint64), ("segments", c_uint64),
-                ("kernel_launches", c_uint64)]
+                ("kernel_launches", c_uint64), ("graph_launches", c_uint64), ("graph_captures", c_uint64)]
 
 
 ST_OK = 0
@@ -110,6 +118,7 @@ _SIGS = {
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),
     "st_adjoint_record": (c_int, [c_void_p, c_int, c_size_t, c_int]),
     "st_adjoint_get_stats": (c_int, [c_void_p, POINTER(AdjointStats)]),
+    "st_ensemble_stats": (c_int, [c_void_p, c_void_p, c_int, POINTER(Ensemble)]),
     "st_adjoint_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     "st_run_noalloc": (c_int, [POINTER(Options), c_int, c_void_p, POINTER(c_size_t), c_int, c_void_p]),
     "st_write_header": (c_int, [c_void_p, POINTER(Options)]),
