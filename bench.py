@@ -222,6 +222,189 @@ def adjoint_timing(args, dev):
             "replays": stats["replays"], "gradients_finite": finite}
 
 
+# ---------------------------------------------------------------- configuration workloads
+# Opt-in lines (--workload); the default run prints only the headline line.
+WORKLOADS = {
+    "sweep": "batched parameter sets: 4096 sets x 256 particles (seed_s = 256 s), per set B0 = (U[1,10] uT, 0, 0), "
+             "9 gradient entries U[0,1e-8] T/m, E_z = +-75e5 V/m, diffuse U[0,0.5], gas collisions at T = 0.4 K, "
+             "sets 0-2047 DOP853 with tf U[0.01,1] s, sets 2048-4095 RK45 with tf U[1e-5,1e-3] s (tf shortened from "
+             "U[1,100] s: RK45 at rtol 1e-12 takes ~20M attempts per particle-second), one window per set",
+    "adjoint50": "adjoint at full length: 65,536 particles, MB 4.2 K, specular walls, gravity, gas off, "
+                 "G ~ N(0,1e-9) T/m, E = (0,0,75e5), B0 = (3e-6,0,0), tf = 50 s, ioutInt 0.5 s; gradients of <Sx>, "
+                 "<Sy> and the mean precession phase; the tape (~1.2 TB) exceeds HBM, so the backward replays "
+                 "window chunks from state checkpoints",
+    "dressing": "spin dressing: 262,144 particles, a = 5e-6 T, w = 2 pi 1000 rad/s (z pulse), B0 = (3e-6,0,0), "
+                "diffuse 0.5, gas collisions at T = 0.4 K, gravity, hmax = 1e-4, tf = 1 s (shortened from 20 s), "
+                "ioutInt 0.5 s",
+    "dressing-grid": "dressing sensitivity: 8 x 8 grid a in [1,10] uT, w in 2 pi [500,2000] rad/s as 64 parameter "
+                     "sets x 4096 particles in one context, otherwise as 'dressing' with tf = 0.2 s; d<P>/d(a, w) of "
+                     "the polarisation P = |<S>| per grid point from one record + one backward pass",
+}
+
+
+def _set_options(n, tf, seed=0, **kw):
+    import spintrack as st
+    f = workload_fields(n, tf)
+    f.update(seed=seed & 0xFFFFFFFF)
+    f.update(kw)
+    return st.derive(apply_fields(st.default_options(), f))
+
+
+def sweep_sets():
+    r = np.random.default_rng(3)
+    sets = []
+    for s in range(4096):
+        dop = s < 2048
+        tf = r.uniform(0.01, 1.0) if dop else r.uniform(1e-5, 1e-3)
+        g = r.uniform(0.0, 1e-8, 9)
+        sets.append(_set_options(256, tf, seed=s * 256, T=0.4, gas_coll=True, diffuse=r.uniform(0.0, 0.5),
+                                 B0=(r.uniform(1e-6, 1e-5), 0.0, 0.0), Gx=tuple(g[0:3]), Gy=tuple(g[3:6]),
+                                 Gz=tuple(g[6:9]), E=(0.0, 0.0, 75e5 if r.uniform() < 0.5 else -75e5), ioutInt=tf,
+                                 integratorType=0 if dop else 1))
+    return sets
+
+
+def dressing_options(n, tf, a=5e-6, w=2 * np.pi * 1000.0):
+    return _set_options(n, tf, T=0.4, gas_coll=True, diffuse=0.5, a=a, w=w, hmax=1e-4,
+                        ioutInt=min(0.5, tf))
+
+
+def _timed_forward(p, nwin, steps, warmup, dev):
+    """Device-timed steps (init + all windows) on the engine's stream."""
+    import torch
+    import spintrack as st
+    stream = torch.cuda.ExternalStream(p.stream(), device=dev)
+
+    def step():
+        p.init_particles()
+        rc = p.run_windows(0, nwin, st.KERNEL_PERSISTENT)
+        if rc != 0:
+            raise RuntimeError(f"run_windows returned {rc}")
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / steps, clk.summary()
+
+
+def run_workload(args):
+    import torch
+    import spintrack as st
+    from spintrack import _capi, workmodel
+    from spintrack.adjoint import NUM_THETA
+    dev = 0
+    torch.cuda.set_device(dev)
+    peak = ctypes.c_double()
+    _capi.check(_capi.load().st_probe_fp64_peak(dev, ctypes.byref(peak)))
+    line = {"workload": args.workload, "description": WORKLOADS[args.workload], "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic"}
+
+    def roofline(counters, secs):
+        ach = workmodel.algorithmic_flops(counters) / secs / 1e12
+        return {"bound": "fp64", "achieved": ach, "peak": peak.value, "unit": "TFLOP/s", "frac": ach / peak.value}
+
+    if args.workload in ("sweep", "dressing"):
+        sets = sweep_sets() if args.workload == "sweep" else [dressing_options(262144, 1.0)]
+        psec = sum(int(o.numParticles) * st.num_windows(o) * o.ioutInt for o in sets)
+        nwin = max(st.num_windows(o) for o in sets)
+        with st.Particles(sets, device=dev) as p:
+            if args.variant >= 0:
+                p.set_launch_config(args.variant, args.bps)
+            secs, clk = _timed_forward(p, nwin, args.steps, 1, dev)
+            c = p.counters()
+            line.update({"metric": "particle*s simulated/s", "value": psec / secs, "unit": "particle*s/s",
+                         "ms_per_step": secs * 1e3, "steps": args.steps, "warmup": 1, "particle_seconds": psec,
+                         "counters": {k: c[k] for k in ("dop_attempts", "rk45_attempts", "segments")},
+                         "roofline": roofline(c, secs), "launch_config": list(p.launch_config()), "clocks": clk})
+            if args.workload == "sweep":
+                half = [sum(int(o.numParticles) * o.tf for o in sets[a:b]) for a, b in ((0, 2048), (2048, 4096))]
+                line["particle_seconds_dop853_rk45"] = half
+        return line
+
+    if args.workload == "adjoint50":
+        g = np.random.default_rng(0).normal(0.0, 1e-9, 9)
+        opt = _set_options(65536, 50.0, diffuse=0.0, Gx=tuple(g[0:3]), Gy=tuple(g[3:6]), Gz=tuple(g[6:9]))
+        sets = [opt]
+    else:
+        av = np.linspace(1e-6, 10e-6, 8)
+        wv = 2 * np.pi * np.linspace(500.0, 2000.0, 8)
+        sets = [dressing_options(4096, 0.2, a=a, w=w) for a in av for w in wv]
+    nwin = max(st.num_windows(o) for o in sets)
+    n = sum(int(o.numParticles) for o in sets)
+    pulse = args.workload == "dressing-grid"
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+    with st.Particles(sets, device=dev) as p:
+        p.init_particles()
+        p.run_windows(0, nwin, st.KERNEL_PERSISTENT)  # tunes the launch configuration
+        p.init_particles()
+        t_fwd = timed(lambda: p.run_windows(0, nwin, st.KERNEL_PERSISTENT))
+        p.init_particles()
+        t_rec = timed(lambda: p.adjoint_record(nwin))
+        stats = p.adjoint_stats()
+        S = torch.empty(n, 3, dtype=torch.float64, device=f"cuda:{dev}")
+        torch.cuda.synchronize()
+        p.gather_spins(S.data_ptr())
+        torch.cuda.synchronize()
+        out = torch.empty(n, NUM_THETA, dtype=torch.float64, device=f"cuda:{dev}")
+        counts = [int(o.numParticles) for o in sets]
+        losses = {}
+        if pulse:
+            w = torch.zeros_like(S)
+            for k, part in enumerate(S.split(counts)):
+                m = part.mean(0)
+                lo = sum(counts[:k])
+                w[lo:lo + counts[k]] = (m / m.norm()) / counts[k]
+            losses["P"] = w
+        else:
+            ok = torch.isfinite(S).all(1)
+            nv = float(ok.sum().item())
+            wx = torch.zeros_like(S)
+            wx[ok, 0] = 1.0 / nv
+            wy = torch.zeros_like(S)
+            wy[ok, 1] = 1.0 / nv
+            r2 = S[:, 1] ** 2 + S[:, 2] ** 2
+            wp = torch.zeros_like(S)
+            wp[ok, 1] = (-S[ok, 2] / r2[ok]) / nv
+            wp[ok, 2] = (S[ok, 1] / r2[ok]) / nv
+            losses = {"Sx": wx, "Sy": wy, "phase": wp}
+        t_bwd = {}
+        grads = {}
+        for name, wgt in losses.items():
+            wgt = wgt.contiguous()
+            t_bwd[name] = timed(lambda: p.adjoint_backward(wgt.data_ptr(), out.data_ptr(), pulse))
+            per_set = torch.stack([c.sum(0) for c in out.split(counts)])
+            grads[name] = per_set.cpu().numpy()
+        bstats = p.adjoint_stats()
+    tb = sum(t_bwd.values()) / len(t_bwd)
+    line.update({"metric": "adjoint seconds", "unit": "s", "particles": n, "windows": nwin,
+                 "forward_batched_s": t_fwd, "record_s": t_rec, "backward_s": t_bwd,
+                 "backward_over_forward": tb / t_fwd, "record_plus_backward_over_forward": (t_rec + tb) / t_fwd,
+                 "tape_gb": stats["tape_bytes_used"] / 1e9, "pool_gb": stats["tape_bytes_pool"] / 1e9,
+                 "tape_resident": bool(stats["resident"]), "checkpoints": stats["checkpoints"],
+                 "replays_per_backward": bstats["replays"], "groups_per_backward": bstats["groups"]})
+    if pulse:
+        g = grads["P"]
+        line["dP_da_grid"] = g[:, 15].reshape(8, 8).tolist()
+        line["dP_dw_grid"] = g[:, 16].reshape(8, 8).tolist()
+        line["gradients_finite"] = bool(np.isfinite(g[:, 15:17]).all())
+    else:
+        line["gradients"] = {k: v[0].tolist() for k, v in grads.items()}
+        line["gradients_finite"] = all(bool(np.isfinite(v).all()) for v in grads.values())
+    return line
+
+
 # ---------------------------------------------------------------- main
 def run_reference(args, world, rank):
     if rank != 0:
@@ -410,7 +593,12 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=None,
+                    help="print the line of one additional configuration instead of the headline line")
     args = ap.parse_args()
+    if args.workload:
+        print(json.dumps(run_workload(args)), flush=True)
+        return 0
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup()

@@ -244,6 +244,21 @@ __device__ __forceinline__ void contract(const SetParams& P, const double p0[3],
 // ---------------------------------------------------------------- backward
 constexpr int kAdjBlock = 64;
 
+// Record the first tape inconsistency (later ones are dropped).
+__device__ void tape_report(const TapeArgs& t, int code, int64_t i, int sp, int si, int gp, int gi, long long ws,
+                            long long wg) {
+  if (atomicCAS(reinterpret_cast<unsigned long long*>(t.error), 0ull, (unsigned long long)code) != 0ull) return;
+  t.error[1] = i;
+  t.error[2] = sp;
+  t.error[3] = si;
+  t.error[4] = gp;
+  t.error[5] = gi;
+  t.error[6] = t.nsteps[i];
+  t.error[7] = t.nsegs[i];
+  t.error[8] = ws;
+  t.error[9] = wg;
+}
+
 // Field polynomial of tape segment record (page, idx).
 __device__ __forceinline__ void tape_load_seg(const TapeArgs& t, const SetParams& P, int page, int idx, Seg& g) {
   const double* r = t.pool + (size_t)page * kTapePageD + (size_t)idx * kTapeSegD;
@@ -272,6 +287,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
   Moments M;
   double lam[3] = {0.0, 0.0, 0.0};
   int sp = -1, si = 0, gp = -1, gi = 0;
+  long long walked_s = 0, walked_g = 0;  // records of the particle's tape walked so far
   while (true) {
     // ---- fetch
     while (!active && !done) {
@@ -283,7 +299,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
       i = a.order ? a.order[item] : (int64_t)item;
       if (t.final_stop[i]) continue;  // stopped particles keep a zero gradient
       if (!t.complete[i]) {
-        atomicExch(t.error, 1);
+        tape_report(t, 1, i, -1, -1, -1, -1, 0, 0);
         continue;
       }
       lam[0] = t.lam[3 * i];
@@ -295,7 +311,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
       gp = t.seg_page[i];
       gi = t.seg_fill[i] - 1;
       if (sp < 0 || sp >= pages || gp < 0 || gp >= pages || si < 0 || gi < 0) {
-        atomicExch(t.error, 2);
+        tape_report(t, 2, i, sp, si, gp, gi, 0, 0);
         continue;
       }
       P = &a.sets[a.s.set[i]];
@@ -305,6 +321,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
 #pragma unroll
       for (int c = 0; c < 3; ++c) M.z0[c] = M.z1[c] = M.z2[c] = 0.0;
       M.ga = M.gw = 0.0;
+      walked_s = walked_g = 0;
       active = true;
     }
     if (__all_sync(FULL, done)) break;
@@ -312,13 +329,15 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
     // ---- one step adjoint
     const double* r = t.pool + (size_t)sp * kTapePageD + (size_t)si * kTapeStepD;
     const double y[3] = {r[0], r[1], r[2]};
-    const double x = r[3], hs = r[4];
-    const bool first = signbit(hs);
-    dop_step_adjoint<kAdjBlock>(g, *P, x, fabs(hs), y, lam, M, pulse, stg);
-    bool finish = false, bad = false;
+    const double x = r[3], h = r[4];
+    const bool first = x == g.t0;  // the segment's first step starts at its t0
+    dop_step_adjoint<kAdjBlock>(g, *P, x, h, y, lam, M, pulse, stg);
+    ++walked_s;
+    bool finish = false;
+    int bad = 0;
     if (--si < 0) {  // chains link to earlier allocated pages: indices strictly decrease
       const int nsp = t.page_prev[sp];
-      bad = nsp >= sp;
+      if (nsp >= sp) bad = 5;
       sp = bad ? -1 : nsp;
       si = kTapeStepsPerPage - 1;
     }
@@ -332,24 +351,33 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
 #pragma unroll
       for (int c = 0; c < 3; ++c) M.z0[c] = M.z1[c] = M.z2[c] = 0.0;
       M.ga = M.gw = 0.0;
+      ++walked_g;
       if (--gi < 0) {
         const int ngp = t.page_prev[gp];
-        gp = (ngp >= gp) ? pages : ngp;  // a link that does not decrease is reported below
+        if (ngp >= gp) bad = 5;
+        gp = ngp;
         gi = kTapeSegsPerPage - 1;
       }
-      if (gp < 0) {
+      if (bad) {
         finish = true;
-        bad = sp >= 0;  // steps left without a segment
-      } else if (gp >= pages || sp < 0 || sp >= pages) {
-        finish = bad = true;
+      } else if (gp < 0) {
+        finish = true;
+        if (sp >= 0) bad = 3;  // steps left without a segment
+      } else if (gp >= pages || sp >= pages) {
+        finish = true;
+        bad = 5;
+      } else if (sp < 0) {
+        finish = true;
+        bad = 4;  // a segment left without steps
       } else {
         tape_load_seg(t, *P, gp, gi, g);
       }
     } else if (sp < 0 || sp >= pages) {
-      finish = bad = true;  // the segment's first step is missing
+      finish = true;
+      bad = sp < 0 ? 6 : 5;  // the segment's first step is missing
     }
     if (finish) {
-      if (bad) atomicExch(t.error, 3);
+      if (bad) tape_report(t, bad, i, sp, si, gp, gi, walked_s, walked_g);
       t.lam[3 * i] = lam[0];
       t.lam[3 * i + 1] = lam[1];
       t.lam[3 * i + 2] = lam[2];

@@ -184,7 +184,7 @@ struct st_ctx {
   int64_t tape_pages = 0;
   void* tape_pp = nullptr;   // per-particle tape arrays, lam and work orders
   unsigned long long* tape_head = nullptr;
-  int* tape_error = nullptr;
+  long long* tape_error = nullptr;
   st::TapeArgs tape{};       // pointers into the above
   int64_t* adj_order = nullptr;   // every particle, longest tape first
   int64_t* adj_gorder = nullptr;  // a group of particles replayed together
@@ -264,16 +264,17 @@ int ctx_alloc(st_ctx* c) {
   return ST_OK;
 }
 
-// Work order for the persistent queue: longest expected particles first
-// (RK45 sets, then by simulated time), so the tail of the run is short.
+// Work order for the persistent queue: longest expected particles first, so
+// the tail of the run is short.  Cost = simulated time, RK45 weighted 2000x
+// (at rtol 1e-12 it takes ~4400x the attempts of DOP853, each ~0.4x the work).
 int ctx_build_order(st_ctx* c) {
   if (c->order_d || c->sets_h.size() <= 1) return ST_OK;
   std::vector<int> idx(c->sets_h.size());
   for (size_t k = 0; k < idx.size(); ++k) idx[k] = (int)k;
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
     const SetParams &A = c->sets_h[a], &B = c->sets_h[b];
-    const double ca = (A.integrator == 1 ? 1000.0 : 1.0) * A.nwin * A.ioutInt;
-    const double cb = (B.integrator == 1 ? 1000.0 : 1.0) * B.nwin * B.ioutInt;
+    const double ca = (A.integrator == 1 ? 2000.0 : 1.0) * A.nwin * A.ioutInt;
+    const double cb = (B.integrator == 1 ? 2000.0 : 1.0) * B.nwin * B.ioutInt;
     return ca > cb;
   });
   std::vector<int64_t> order;
@@ -869,7 +870,7 @@ int adj_alloc_particle_arrays(st_ctx* c) {
   c->adj_order = (int64_t*)ptr[8];
   c->adj_gorder = (int64_t*)ptr[9];
   ST_CUDA(cudaMalloc(&c->tape_head, sizeof(unsigned long long)));
-  ST_CUDA(cudaMalloc(&c->tape_error, sizeof(int)));
+  ST_CUDA(cudaMalloc(&c->tape_error, sizeof(long long) * st::kTapeErrorSlots));
   t.pool_head = c->tape_head;
   t.error = c->tape_error;
   return ST_OK;
@@ -887,7 +888,7 @@ int adj_reset_tape(st_ctx* c) {
   ST_CUDA(cudaMemsetAsync(t.nsteps, 0, 8 * m, c->stream));
   ST_CUDA(cudaMemsetAsync(t.nsegs, 0, 8 * m, c->stream));
   ST_CUDA(cudaMemsetAsync(c->tape_head, 0, sizeof(unsigned long long), c->stream));
-  ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(int), c->stream));
+  ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(long long) * st::kTapeErrorSlots, c->stream));
   return ST_OK;
 }
 
@@ -903,11 +904,22 @@ int adj_backward_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) 
   const int per_sm = std::max(1, st::adj_backward_max_blocks_per_sm());
   int e = st::launch_adj_backward(a, t, c->sm_count * per_sm, c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("adjoint backward launch: ") + cudaGetErrorString((cudaError_t)e));
-  int bad = 0;
-  ST_CUDA(cudaMemcpyAsync(&bad, c->tape_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  long long rep[st::kTapeErrorSlots] = {};
+  ST_CUDA(cudaMemcpyAsync(rep, c->tape_error, sizeof(rep), cudaMemcpyDeviceToHost, c->stream));
   cudaError_t se = cudaStreamSynchronize(c->stream);
   if (se != cudaSuccess) return fail(ST_ERR_CUDA, std::string("adjoint backward: ") + cudaGetErrorString(se));
-  if (bad) return fail(ST_ERR_CUDA, "internal: the adjoint tape was inconsistent (code " + std::to_string(bad) + ")");
+  if (rep[0]) {
+    static const char* what[] = {"", "a particle's tape was not stored in full", "bad chain heads",
+                                 "steps left after the first segment", "a segment without steps",
+                                 "a page link out of range", "a segment's first step missing"};
+    std::string m = "internal: the adjoint tape was inconsistent: ";
+    m += (rep[0] > 0 && rep[0] < 7) ? what[rep[0]] : "?";
+    m += " (particle " + std::to_string(rep[1]) + ", step page/record " + std::to_string(rep[2]) + "/" +
+         std::to_string(rep[3]) + ", segment page/record " + std::to_string(rep[4]) + "/" + std::to_string(rep[5]) +
+         ", tape " + std::to_string(rep[6]) + " steps " + std::to_string(rep[7]) + " segments, walked " +
+         std::to_string(rep[8]) + " steps " + std::to_string(rep[9]) + " segments)";
+    return fail(ST_ERR_CUDA, m);
+  }
   return ST_OK;
 }
 
@@ -1149,7 +1161,7 @@ int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags)
   t.pulse_grads = (flags & 1) ? 1 : 0;
   ST_CUDA(cudaMemcpyAsync(t.lam, dL_dS, 24 * n, cudaMemcpyDeviceToDevice, c->stream));
   ST_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * st::kNumTheta * n, c->stream));
-  ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(int), c->stream));
+  ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(long long) * st::kTapeErrorSlots, c->stream));
   if (c->adj_resident) {
     st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
     a.order = c->adj_order;
@@ -1413,26 +1425,34 @@ int autotune(st_ctx* c) {
     return ST_OK;
   }
   const int nv = st::persistent_variant_count();
-  // Sample: enough particles to fill two rounds of lanes, every set
-  // represented, one short window (ioutInt capped at 20 ms) on a scratch
-  // context, so each candidate runs for a few milliseconds.
+  // Sample: every set represented, about four particles per lane of the
+  // widest candidate (one particle per lane would let the slowest particle
+  // decide and favour low occupancy), one short window on a scratch context,
+  // so each candidate runs for tens of milliseconds: the window is capped at
+  // 50 ms of simulated time for DOP853 sets (~250 attempts per particle at
+  // rtol 1e-12) and at 50 us for RK45 sets, whose step at rtol 1e-12 is
+  // thousands of times shorter.
   std::vector<st_options> sample = c->opts;
-  const int64_t want = std::max<int64_t>((int64_t)c->sm_count * 512, 1);
+  int widest = 1;
+  for (int v = 0; v < nv; ++v)
+    widest = std::max(widest, st::persistent_max_blocks_per_sm(v, 0) * st::persistent_variant_block(v));
+  const int64_t want = std::max<int64_t>((int64_t)c->sm_count * widest * 4, 1);
   const double frac = std::min(1.0, (double)want / (double)std::max<int64_t>(c->n, 1));
   for (auto& o : sample) {
     o.numParticles = o.numParticles > 0 ? std::max(1, (int)std::ceil(o.numParticles * frac)) : 0;
-    o.ioutInt = std::min(o.ioutInt, 0.02);
+    o.ioutInt = std::min(o.ioutInt, o.integratorType == 1 ? 5e-5 : 0.05);
     o.tf = o.t0 + o.ioutInt;
   }
   st_ctx* s = nullptr;
   ST_TRY(st_create_batch(sample.data(), (int)sample.size(), c->device, &s));
   double best = 1e300;
   st_launch_config best_cfg{0, 1, 1};
+  // Each variant at its highest occupancy (its register budget is part of
+  // the variant): on every workload measured, fewer resident blocks lost.
   for (int v = 0; v < nv; ++v) {
     const int maxb = std::max(1, st::persistent_max_blocks_per_sm(v, 0));
-    const int cands[2] = {1, maxb};
-    for (int k = 0; k < (maxb > 1 ? 2 : 1); ++k) {
-      st_launch_config cfg{0, cands[k], v};
+    {
+      st_launch_config cfg{0, maxb, v};
       st_set_launch_config(s, &cfg);
       double el = 1e300;
       for (int rep = 0; rep < 2; ++rep) {  // first repetition warms the variant up

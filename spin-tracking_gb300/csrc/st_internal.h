@@ -103,11 +103,19 @@ constexpr int kNumTheta = 17;
 // The adjoint's tape, written by the trajectory-ahead kernel (k_batched with
 // its tape switch on): pages of kTapePageD doubles from one pool.  Every
 // particle owns two chains of pages, linked last to first: its accepted
-// DOP853 steps (y, x, h; h negated on the first step of a segment) and its
-// integrated segments (t0, p0, v0).
+// DOP853 steps (y, x, h) and its integrated segments (t0, p0, v0).  A step
+// is the first of its segment exactly when x equals the segment's t0: the
+// first accepted step starts at t0 (rejected attempts do not move x), and
+// later steps cannot return there (a zero-length segment has one step).  The
+// sign of h carries no flag: a segment shorter than hmin is overshot by an
+// hmin step and closed by a negative one, as in the reference.
 constexpr int kTapePageD = 320;
 constexpr int kTapeStepD = 5, kTapeStepsPerPage = 64;
 constexpr int kTapeSegD = 8, kTapeSegsPerPage = 40;
+// Tape consistency report: [0] code (0 = none), [1] particle, [2..5] step page,
+// step record, segment page, segment record, [6..7] steps and segments of the
+// particle's tape, [8..9] steps and segments walked back when it was found.
+constexpr int kTapeErrorSlots = 10;
 struct TapeArgs {
   double* pool;
   int32_t* page_prev;             // per page: the chain's previous page (-1: none)
@@ -128,7 +136,7 @@ struct TapeArgs {
   double* grad;                   // per particle: kNumTheta accumulators (+=)
   const uint8_t* final_stop;      // per particle: stopped at the end of the forward run
   int pulse_grads;
-  int* error;                     // set by a kernel that found an inconsistent tape
+  long long* error;               // kTapeErrorSlots: first inconsistency found (code, particle, cursors)
 };
 // The trajectory-ahead kernel with its tape switch on (st_kernels.cu).
 int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);
@@ -163,6 +171,7 @@ int build_set_params(const st_options& o, int64_t first, SetParams* P);
 int set_last_error(int code, const char* msg);
 int persistent_max_blocks_per_sm(int variant, int block);
 int persistent_prepare(int variant);
+int persistent_variant_block(int variant);
 const char* persistent_variant_name(int variant);
 
 }  // namespace st

@@ -462,7 +462,6 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   const unsigned long long dl = run_deadline(a);
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   TapeCursor tc;
-  bool seg_first = false;  // no step of the open segment accepted yet
   tape_open(tc);
   DiffuseDefer dd;
   dd.pending = false;
@@ -533,7 +532,6 @@ __global__ void __launch_bounds__(BLOCK, MINB)
             dop_begin(g, *P, tp.Sx, tp.Sy, tp.Sz, tempH);
           else
             rk45_begin(g, tempH);
-          seg_first = true;
           mode = B_SEG;
           break;
         } else {  // trajectory only: the segment completes at once
@@ -618,10 +616,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
         const double y0x = tp.Sx, y0y = tp.Sy, y0z = tp.Sz, x0 = g.x;
         r = dop_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
         ++n_dop;
-        if (TAPE && g.acc) {
-          tape_step(ta, tc, y0x, y0y, y0z, x0, seg_first ? -g.hu : g.hu);
-          seg_first = false;
-        }
+        if (TAPE && g.acc) tape_step(ta, tc, y0x, y0y, y0z, x0, g.hu);
       } else {
         r = rk45_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
         ++n_rk;
@@ -759,6 +754,7 @@ static const Variant kVariants[] = {
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int persistent_variant_count() { return kNumVariants; }
+int persistent_variant_block(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].block : 0; }
 const char* persistent_variant_name(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "?"; }
 
 template <bool GAS>

@@ -193,3 +193,35 @@ def test_backward_is_independent_of_the_tape_budget(gpu):
     assert np.all(np.isfinite(g_res))
     np.testing.assert_allclose(g_chunk, g_res, rtol=1e-12, atol=1e-300)
     np.testing.assert_allclose(g_grp, g_res, rtol=1e-12, atol=1e-300)
+
+
+def overshoot_options():
+    """One particle (index 2412 of a seed-0 run) in a 1 kHz dressing field
+    with gas collisions at 0.4 K and hmax 1e-4: one of its segments is
+    shorter than hmin, so the step controller steps hmin past the segment end
+    and closes the segment with a negative step, as the reference does."""
+    g = np.random.default_rng(0).normal(0.0, 1e-9, 9)
+    return st.derive(st.make_options(numParticles=1, dist="M", T=0.4, diffuse=0.5, gas_coll=True, gravity=True,
+                                     Gx=g[0:3], Gy=g[3:6], Gz=g[6:9], E=(0.0, 0.0, 75e5), B0=(3e-6, 0.0, 0.0),
+                                     yi=(0.0, 0.0, 1.0), tf=0.2, ioutInt=0.2, seed=2412, rtol=1e-12, atol=1e-12,
+                                     h=1e-3, hmax=1e-4, hmin=1e-8, a=5e-6, w=2 * math.pi * 1000.0))
+
+
+def test_adjoint_through_an_hmin_overshoot(gpu, oracle):
+    from _oracle import Options
+    opt = overshoot_options()
+    log = np.zeros(2 * 200_000)
+    oracle.L.or_set_step_log(log.ctypes.data_as(ctypes.c_void_p), log.shape[0] // 2, 1)
+    try:
+        oracle.run_sample(Options.from_buffer_copy(bytes(opt)), 0, 1, threads=1)
+        n = int(oracle.L.or_step_log_count())
+    finally:
+        oracle.L.or_set_step_log(None, 0, 0)
+    assert n > 0 and np.any(log[0:2 * n:2] < 0.0)  # the case is exercised: a negative accepted step
+    W = np.random.default_rng(5).normal(size=(1, 3))
+    g, S = gpu_grad(opt, W, True)
+    fd, base = frozen_fd(oracle, opt, W, True)
+    assert np.max(np.abs(S - base["S"])) <= 1e-9
+    bad = [f"{THETA_NAMES[k]} adj={g[k]:.10e} fd={fd[k]:.10e}" for k in range(NUM_THETA)
+           if abs(g[k] - fd[k]) > 1e-6 * abs(fd[k]) + 1e-14 * np.max(np.abs(fd))]
+    assert not bad, "\n".join(bad)
