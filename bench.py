@@ -236,6 +236,10 @@ WORKLOADS = {
     "dressing": "spin dressing: 262,144 particles, a = 5e-6 T, w = 2 pi 1000 rad/s (z pulse), B0 = (3e-6,0,0), "
                 "diffuse 0.5, gas collisions at T = 0.4 K, gravity, hmax = 1e-4, tf = 1 s (shortened from 20 s), "
                 "ioutInt 0.5 s",
+    "adjoint-small": "adjoint, small case for profiles: 65,536 particles (the lanes of the backward as full), MB "
+                     "4.2 K, specular walls, gravity, gas off, G ~ N(0,1e-9) T/m, E = (0,0,75e5), B0 = (3e-6,0,0), "
+                     "tf = 0.05 s, tape pool 3 GB (the tape, ~0.9 GB, stays resident); gradients of <Sx>, <Sy> and "
+                     "the mean precession phase",
     "dressing-grid": "dressing sensitivity: 8 x 8 grid a in [1,10] uT, w in 2 pi [500,2000] rad/s as 64 parameter "
                      "sets x 4096 particles in one context, otherwise as 'dressing' with tf = 0.2 s; d<P>/d(a, w) of "
                      "the polarisation P = |<S>| per grid point from one record + one backward pass",
@@ -327,10 +331,14 @@ def run_workload(args):
                 line["particle_seconds_dop853_rk45"] = half
         return line
 
-    if args.workload == "adjoint50":
+    tape_bytes = 0
+    if args.workload in ("adjoint50", "adjoint-small"):
         g = np.random.default_rng(0).normal(0.0, 1e-9, 9)
-        opt = _set_options(65536, 50.0, diffuse=0.0, Gx=tuple(g[0:3]), Gy=tuple(g[3:6]), Gz=tuple(g[6:9]))
+        small = args.workload == "adjoint-small"
+        opt = _set_options(65536, 0.05 if small else 50.0, diffuse=0.0, Gx=tuple(g[0:3]), Gy=tuple(g[3:6]),
+                           Gz=tuple(g[6:9]), ioutInt=0.05 if small else 0.5)
         sets = [opt]
+        tape_bytes = 3_000_000_000 if small else 0
     else:
         av = np.linspace(1e-6, 10e-6, 8)
         wv = 2 * np.pi * np.linspace(500.0, 2000.0, 8)
@@ -351,7 +359,7 @@ def run_workload(args):
         p.init_particles()
         t_fwd = timed(lambda: p.run_windows(0, nwin, st.KERNEL_PERSISTENT))
         p.init_particles()
-        t_rec = timed(lambda: p.adjoint_record(nwin))
+        t_rec = timed(lambda: p.adjoint_record(nwin, tape_bytes=tape_bytes))
         stats = p.adjoint_stats()
         S = torch.empty(n, 3, dtype=torch.float64, device=f"cuda:{dev}")
         torch.cuda.synchronize()
@@ -505,13 +513,11 @@ def run_ours(args, world, rank, local):
                            "nominal GB300 FP64 1.25 TFLOP/s)",
             "work_per_launch": {"dop_attempts": counters["dop_attempts"], "segments": counters["segments"],
                                 "flops": flops, "kernel_ms": kernel_s * 1e3}}
-    tr = REPO / "profiles" / "traffic.json"
-    if tr.exists():
-        try:
-            t = json.loads(tr.read_text())
-            roof["traffic"] = t.get("bytes_per_launch_scaled")
-        except Exception:
-            pass
+    # DRAM bytes of one launch, from an ncu capture of the same kernel on 65,536 particles of this
+    # workload (dram__bytes_read + write = 11.67 MB + 0, profiles/k_batched_bench_65k_full.md):
+    # 178 B per particle (its state, read once), scaled to this launch's particles.
+    roof["traffic"] = 178.0 * n
+    roof["traffic_source"] = "ncu capture of 65,536 particles (178 B per particle), scaled to this launch"
 
     # ---- plain one-thread-per-particle kernel on the same workload (1 step)
     plain = None
