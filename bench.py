@@ -395,13 +395,22 @@ def run_workload(args):
             per_set = torch.stack([c.sum(0) for c in out.split(counts)])
             grads[name] = per_set.cpu().numpy()
         bstats = p.adjoint_stats()
+        t_multi = None
+        if len(losses) > 1:  # all losses in one backward: one replay per chunk serves them all
+            wall = torch.stack([w.contiguous() for w in losses.values()]).contiguous()
+            outm = torch.empty(len(losses), n, NUM_THETA, dtype=torch.float64, device=f"cuda:{dev}")
+            t_multi = timed(lambda: p.adjoint_backward_multi(len(losses), wall.data_ptr(), outm.data_ptr(), pulse))
+            for k, name in enumerate(losses):
+                assert np.array_equal(torch.stack([c.sum(0) for c in outm[k].split(counts)]).cpu().numpy(),
+                                      grads[name])
     tb = sum(t_bwd.values()) / len(t_bwd)
     line.update({"metric": "adjoint seconds", "unit": "s", "particles": n, "windows": nwin,
                  "forward_batched_s": t_fwd, "record_s": t_rec, "backward_s": t_bwd,
                  "backward_over_forward": tb / t_fwd, "record_plus_backward_over_forward": (t_rec + tb) / t_fwd,
                  "tape_gb": stats["tape_bytes_used"] / 1e9, "pool_gb": stats["tape_bytes_pool"] / 1e9,
                  "tape_resident": bool(stats["resident"]), "checkpoints": stats["checkpoints"],
-                 "replays_per_backward": bstats["replays"], "groups_per_backward": bstats["groups"]})
+                 "replays_per_backward": bstats["replays"], "groups_per_backward": bstats["groups"],
+                 "backward_all_losses_one_call_s": t_multi})
     if pulse:
         g = grads["P"]
         line["dP_da_grid"] = g[:, 15].reshape(8, 8).tolist()

@@ -221,6 +221,11 @@ int st_adjoint_record(st_ctx *ctx, int w_end, size_t tape_bytes, int windows_per
  * the set's gradient.  Particles that stopped (failure codes) get zeros.
  * flags bit 0: also differentiate the pulse (a, w), one sincos per stage. */
 int st_adjoint_backward(st_ctx *ctx, const double *dL_dS, double *grad, int flags);
+/* The backward for nloss losses at once: dL_dS holds nloss blocks of
+ * 3 doubles per particle, grad receives nloss blocks of ST_NUM_THETA doubles
+ * per particle.  When the tape did not fit, each chunk of the run is replayed
+ * once for all the losses.  No counterpart in the reference. */
+int st_adjoint_backward_multi(st_ctx *ctx, int nloss, const double *dL_dS, double *grad, int flags);
 /* What the last record / backward pair did (no reference counterpart). */
 typedef struct {
   uint64_t tape_bytes_used;   /* tape written by the record pass (all of it, stored or not) */

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "spintrack.h"
@@ -182,7 +183,7 @@ struct st_ctx {
   double* tape_pool = nullptr;
   int32_t* tape_prev = nullptr;
   int64_t tape_pages = 0;
-  void* tape_pp = nullptr;   // per-particle tape arrays, lam and work orders
+  void* tape_pp = nullptr;   // per-particle tape arrays and work orders
   unsigned long long* tape_head = nullptr;
   long long* tape_error = nullptr;
   st::TapeArgs tape{};       // pointers into the above
@@ -194,6 +195,10 @@ struct st_ctx {
   void* replay_arena = nullptr;   // state of a replay
   std::vector<int64_t> adj_nsteps_h, adj_nsegs_h;
   std::vector<uint8_t> adj_stop_h;
+  double* adj_lam_buf = nullptr;  // per loss and particle: the spin adjoint carried between chunks
+  size_t adj_lam_cap = 0;          // doubles allocated
+  int adj_nloss = 1;               // losses of the running backward
+  double* adj_grad_base = nullptr; // their gradients, loss after loss
   int adj_w_end = 0;
   int adj_w_run = 0;              // windows the record pass ran (w_end capped at the sets' windows)
   bool adj_recorded = false;
@@ -264,15 +269,21 @@ int ctx_alloc(st_ctx* c) {
   return ST_OK;
 }
 
-// Work order for the persistent queue: longest expected particles first, so
-// the tail of the run is short.  Cost = simulated time, RK45 weighted 2000x
-// (at rtol 1e-12 it takes ~4400x the attempts of DOP853, each ~0.4x the work).
+// Work order for the persistent queue: sets grouped by integrator (RK45,
+// then DOP853, then trajectory-only), so that a warp's lanes run one step code
+// and do not diverge between two; within a group, longest expected particles
+// first, so the tail of the run is short.  Cost = simulated time, RK45
+// weighted 2000x (at rtol 1e-12 it takes ~4400x the attempts of DOP853, each
+// ~0.4x the work).
 int ctx_build_order(st_ctx* c) {
   if (c->order_d || c->sets_h.size() <= 1) return ST_OK;
   std::vector<int> idx(c->sets_h.size());
   for (size_t k = 0; k < idx.size(); ++k) idx[k] = (int)k;
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
     const SetParams &A = c->sets_h[a], &B = c->sets_h[b];
+    const int ga = A.integrator == 1 ? 0 : (A.integrator == 0 ? 1 : 2);
+    const int gb = B.integrator == 1 ? 0 : (B.integrator == 0 ? 1 : 2);
+    if (ga != gb) return ga < gb;
     const double ca = (A.integrator == 1 ? 2000.0 : 1.0) * A.nwin * A.ioutInt;
     const double cb = (B.integrator == 1 ? 2000.0 : 1.0) * B.nwin * B.ioutInt;
     return ca > cb;
@@ -583,6 +594,7 @@ void st_destroy(st_ctx* c) {
   cudaFree(c->order_d);
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   cudaFree(c->ens_buf);
+  cudaFree(c->adj_lam_buf);
   cudaFree(c->tape_pool);
   cudaFree(c->tape_prev);
   cudaFree(c->tape_pp);
@@ -847,14 +859,14 @@ inline int64_t tape_pages_for(int64_t steps, int64_t segs) {
 int adj_alloc_particle_arrays(st_ctx* c) {
   if (c->tape_pp) return ST_OK;
   const size_t m = (size_t)std::max<int64_t>(c->n, 1);
-  const size_t sz[] = {4 * m, 4 * m, 4 * m, 4 * m, 4 * m, 8 * m, 8 * m, 24 * m, 8 * m, 8 * m};
+  const size_t sz[] = {4 * m, 4 * m, 4 * m, 4 * m, 4 * m, 8 * m, 8 * m, 8 * m, 8 * m};
   size_t total = 0;
   for (size_t x : sz) total += align256(x);
   cudaError_t e = cudaMalloc(&c->tape_pp, total);
   if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint arrays: ") + cudaGetErrorString(e));
   char* p = (char*)c->tape_pp;
-  void* ptr[10];
-  for (int k = 0; k < 10; ++k) {
+  void* ptr[9];
+  for (int k = 0; k < 9; ++k) {
     ptr[k] = p;
     p += align256(sz[k]);
   }
@@ -866,9 +878,8 @@ int adj_alloc_particle_arrays(st_ctx* c) {
   t.complete = (int32_t*)ptr[4];
   t.nsteps = (int64_t*)ptr[5];
   t.nsegs = (int64_t*)ptr[6];
-  t.lam = (double*)ptr[7];
-  c->adj_order = (int64_t*)ptr[8];
-  c->adj_gorder = (int64_t*)ptr[9];
+  c->adj_order = (int64_t*)ptr[7];
+  c->adj_gorder = (int64_t*)ptr[8];
   ST_CUDA(cudaMalloc(&c->tape_head, sizeof(unsigned long long)));
   ST_CUDA(cudaMalloc(&c->tape_error, sizeof(long long) * st::kTapeErrorSlots));
   t.pool_head = c->tape_head;
@@ -943,6 +954,18 @@ int adj_upload_order(st_ctx* c, const std::vector<int64_t>& ids, int64_t* dst) {
   return ST_OK;
 }
 
+// The backward over the tape in the pool, once per loss of the running
+// backward (each loss has its own spin adjoints and gradient block).
+int adj_backward_losses(st_ctx* c, const st::RunArgs& ab, st::TapeArgs t) {
+  const size_t n = (size_t)c->n;
+  for (int l = 0; l < c->adj_nloss; ++l) {
+    t.lam = c->adj_lam_buf + 3 * n * (size_t)l;
+    t.grad = c->adj_grad_base + (size_t)st::kNumTheta * n * (size_t)l;
+    ST_TRY(adj_backward_launch(c, ab, t));
+  }
+  return ST_OK;
+}
+
 // Replay windows up to b_hi from checkpoint slot `slot` for the particles of
 // `group` (nullptr: all), writing their tape; then run the backward over
 // them.  Sets *fitted = false (and runs no backward) when the tape did not fit.
@@ -979,7 +1002,7 @@ int adj_replay_and_back(st_ctx* c, int slot, int b_hi, const std::vector<int64_t
   st::RunArgs ab = make_args(c, 0, b_hi, nullptr);
   ab.order = group ? c->adj_gorder : c->adj_order;
   ab.nitems = a.nitems;
-  return adj_backward_launch(c, ab, t);
+  return adj_backward_losses(c, ab, t);  // one replay serves every loss
 }
 
 // One chunk of checkpoint intervals [k_lo, k_hi), last chunk of the run first;
@@ -1148,25 +1171,40 @@ int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_c
 }
 
 int st_adjoint_backward(st_ctx* c, const double* dL_dS, double* grad, int flags) {
+  return st_adjoint_backward_multi(c, 1, dL_dS, grad, flags);
+}
+
+int st_adjoint_backward_multi(st_ctx* c, int nloss, const double* dL_dS, double* grad, int flags) {
   if (!c || !dL_dS || !grad) return fail(ST_ERR_ARG, "null argument");
+  if (nloss < 1) return fail(ST_ERR_ARG, "nloss must be at least 1");
   if (!c->adj_recorded) return fail(ST_ERR_STATE, "st_adjoint_backward needs st_adjoint_record first");
   ST_CUDA(cudaSetDevice(c->device));
   const size_t n = (size_t)c->n;
   c->adj_stats.replays = 0;
   c->adj_stats.groups = 0;
   if (n == 0) return ST_OK;
+  const size_t lam_d = 3 * n * (size_t)nloss;
+  if (lam_d > c->adj_lam_cap) {
+    cudaFree(c->adj_lam_buf);
+    c->adj_lam_buf = nullptr;
+    c->adj_lam_cap = 0;
+    cudaError_t e = cudaMalloc(&c->adj_lam_buf, sizeof(double) * lam_d);
+    if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint spin adjoints: ") + cudaGetErrorString(e));
+    c->adj_lam_cap = lam_d;
+  }
+  c->adj_nloss = nloss;
+  c->adj_grad_base = grad;
   st::TapeArgs t = adj_tape_args(c);
-  t.grad = grad;
   t.final_stop = c->s.stop;
   t.pulse_grads = (flags & 1) ? 1 : 0;
-  ST_CUDA(cudaMemcpyAsync(t.lam, dL_dS, 24 * n, cudaMemcpyDeviceToDevice, c->stream));
-  ST_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * st::kNumTheta * n, c->stream));
+  ST_CUDA(cudaMemcpyAsync(c->adj_lam_buf, dL_dS, sizeof(double) * lam_d, cudaMemcpyDeviceToDevice, c->stream));
+  ST_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * st::kNumTheta * n * (size_t)nloss, c->stream));
   ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(long long) * st::kTapeErrorSlots, c->stream));
   if (c->adj_resident) {
     st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
     a.order = c->adj_order;
     a.nitems = c->n;
-    return adj_backward_launch(c, a, t);
+    return adj_backward_losses(c, a, t);
   }
   // replay chunks of checkpoint intervals, last first, each sized from the
   // record pass's tape length (time-uniform estimate; halves when it misses)
@@ -1348,13 +1386,15 @@ extern "C" int st_main_analysis(const st_options* opt_in, const char* out_path, 
     FILE* f;
     void* snap_d;
     void* snap_h;
+    std::thread writer;  // writes one chunk of snapshots while the next one runs
     ~Guard() {
+      if (writer.joinable()) writer.join();
       if (f) std::fclose(f);
       if (snap_d) cudaFree(snap_d);
       if (snap_h) cudaFreeHost(snap_h);
       st_destroy(c);
     }
-  } g{c, nullptr, nullptr, nullptr};
+  } g{c, nullptr, nullptr, nullptr, std::thread()};
   ST_TRY(st_init(c));
   g.f = std::fopen(out_path, "wb");
   if (!g.f) return fail(ST_ERR_IO, std::string("cannot open ") + out_path);
@@ -1375,24 +1415,41 @@ extern "C" int st_main_analysis(const st_options* opt_in, const char* out_path, 
       ST_TRY(st_write_snapshot(g.f, (int)n, &hv));
     }
   } else {
-    // windows in chunks whose snapshot blocks fit a quarter of free memory
+    // Windows in chunks whose snapshot blocks take at most a quarter of free
+    // device memory and 2 GiB.  Two pinned host buffers: while the GPU runs
+    // chunk k + 1, a writer thread unpacks and writes chunk k (in window
+    // order); only the device-to-host copy of each chunk is serial.
     size_t free_b = 0, total_b = 0;
     ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t blk = st_snapshot_bytes(c);
-    int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nwin, 1), (free_b / 4) / std::max<size_t>(blk, 1)));
+    const size_t blk = std::max<size_t>(st_snapshot_bytes(c), 1);
+    const size_t cap = std::min<size_t>(free_b / 4, (size_t)2 << 30);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nwin, 1), cap / blk));
     ST_CUDA(cudaMalloc(&g.snap_d, blk * (size_t)chunk));
-    ST_CUDA(cudaMallocHost(&g.snap_h, blk * (size_t)chunk));
+    ST_CUDA(cudaMallocHost(&g.snap_h, 2 * blk * (size_t)chunk));
+    int werr = 0;  // set by the writer, read after joining it
+    int slot = 0;
     for (int w = 0; w < nwin; w += chunk) {
       const int we = std::min(nwin, w + chunk);
       const double t0 = now_s();
       ST_TRY(st_run_windows(c, kernel, w, we, g.snap_d));
       run += now_s() - t0;
-      ST_CUDA(cudaMemcpy(g.snap_h, g.snap_d, blk * (size_t)(we - w), cudaMemcpyDeviceToHost));
-      for (int k = 0; k < we - w; ++k) {
-        unpack_block(c, (const char*)g.snap_h + blk * (size_t)k, hs);
-        ST_TRY(st_write_snapshot(g.f, (int)n, &hv));
-      }
+      // the writer that last used this buffer finished before the previous chunk was handed over
+      char* hb = (char*)g.snap_h + (size_t)slot * blk * (size_t)chunk;
+      ST_CUDA(cudaMemcpy(hb, g.snap_d, blk * (size_t)(we - w), cudaMemcpyDeviceToHost));
+      if (g.writer.joinable()) g.writer.join();
+      if (werr) return fail(ST_ERR_IO, "snapshot write failed");
+      const int count = we - w;
+      g.writer = std::thread([c, hb, count, blk, n, &hs, &werr, f = g.f]() {
+        st_state_view v = hs.view();
+        for (int k = 0; k < count && !werr; ++k) {
+          unpack_block(c, hb + blk * (size_t)k, hs);
+          if (st_write_snapshot(f, (int)n, &v) != ST_OK) werr = 1;
+        }
+      });
+      slot ^= 1;
     }
+    if (g.writer.joinable()) g.writer.join();
+    if (werr) return fail(ST_ERR_IO, "snapshot write failed");
   }
   if (run_seconds) *run_seconds = run;
   return ST_OK;

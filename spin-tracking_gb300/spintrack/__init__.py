@@ -184,6 +184,12 @@ class Particles:
         check(load().st_adjoint_get_stats(self._ctx, ctypes.byref(s)))
         return {k: int(getattr(s, k)) for k, _ in AdjointStats._fields_ if k != "pad"}
 
+    def adjoint_backward_multi(self, nloss: int, dLdS_ptr: int, grad_ptr: int, pulse: bool = False) -> None:
+        """nloss blocks of dL/dS (device, 3 doubles per particle each) -> nloss blocks of dL/dtheta
+        (device, 17 doubles per particle each); one replay of the run serves all of them."""
+        check(load().st_adjoint_backward_multi(self._ctx, int(nloss), ctypes.c_void_p(dLdS_ptr),
+                                               ctypes.c_void_p(grad_ptr), 1 if pulse else 0))
+
     def adjoint_backward(self, dLdS_ptr: int, grad_ptr: int, pulse: bool = False) -> None:
         """dL/dS (device, 3 doubles per particle) -> dL/dtheta per particle (device, 17 doubles)."""
         check(load().st_adjoint_backward(self._ctx, ctypes.c_void_p(dLdS_ptr), ctypes.c_void_p(grad_ptr),

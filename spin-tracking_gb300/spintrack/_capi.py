@@ -120,6 +120,7 @@ _SIGS = {
     "st_adjoint_get_stats": (c_int, [c_void_p, POINTER(AdjointStats)]),
     "st_ensemble_stats": (c_int, [c_void_p, c_void_p, c_int, POINTER(Ensemble)]),
     "st_adjoint_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
+    "st_adjoint_backward_multi": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int]),
     "st_run_noalloc": (c_int, [POINTER(Options), c_int, c_void_p, POINTER(c_size_t), c_int, c_void_p]),
     "st_write_header": (c_int, [c_void_p, POINTER(Options)]),
     "st_write_snapshot": (c_int, [c_void_p, c_int, POINTER(StateView)]),

@@ -225,3 +225,36 @@ def test_adjoint_through_an_hmin_overshoot(gpu, oracle):
     bad = [f"{THETA_NAMES[k]} adj={g[k]:.10e} fd={fd[k]:.10e}" for k in range(NUM_THETA)
            if abs(g[k] - fd[k]) > 1e-6 * abs(fd[k]) + 1e-14 * np.max(np.abs(fd))]
     assert not bad, "\n".join(bad)
+
+
+def test_multi_loss_backward_equals_single_loss_calls(gpu):
+    """st_adjoint_backward_multi with three losses gives, bit for bit, the
+    gradients of three single-loss backward calls, with the tape resident and
+    with window-chunk replays, where one replay of each chunk serves all three
+    losses (as many replays as one single-loss call)."""
+    import torch
+    opt = adj_options(n=16, tf=0.2)
+    nw = st.num_windows(opt)
+    W = torch.tensor(np.random.default_rng(8).normal(size=(3, 16, 3)), dtype=torch.float64, device="cuda")
+    with st.Particles(opt) as p:
+        used = None
+        for resident in (True, False):
+            budget = 0 if resident else used // 2
+            p.init_particles()
+            p.adjoint_record(nw, tape_bytes=budget, windows_per_checkpoint=1)
+            if resident:
+                used = p.adjoint_stats()["tape_bytes_used"]
+            out_m = torch.empty(3, 16, NUM_THETA, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            p.adjoint_backward_multi(3, W.data_ptr(), out_m.data_ptr())
+            torch.cuda.synchronize()
+            rep_multi = p.adjoint_stats()["replays"]
+            assert rep_multi == 0 if resident else rep_multi >= 2
+            for l in range(3):
+                out = torch.empty(16, NUM_THETA, dtype=torch.float64, device="cuda")
+                wl = W[l].contiguous()
+                torch.cuda.synchronize()
+                p.adjoint_backward(wl.data_ptr(), out.data_ptr())
+                torch.cuda.synchronize()
+                assert torch.equal(out, out_m[l]), f"loss {l}, resident={resident}"
+                assert p.adjoint_stats()["replays"] == rep_multi
