@@ -258,3 +258,25 @@ def test_multi_loss_backward_equals_single_loss_calls(gpu):
                 torch.cuda.synchronize()
                 assert torch.equal(out, out_m[l]), f"loss {l}, resident={resident}"
                 assert p.adjoint_stats()["replays"] == rep_multi
+
+
+def test_stopped_particles_get_zero_gradients(gpu):
+    """Particles that fail (here: DOP853 over nmax attempts in a segment)
+    contribute nothing; the others are unaffected by their presence."""
+    import torch
+    opt = adj_options(n=32, tf=0.1)
+    opt.nmax = 10  # segments needing more attempts fail with code -1 (2 of these 32 particles)
+    nw = st.num_windows(opt)
+    with st.Particles(opt) as p:
+        p.init_particles()
+        p.adjoint_record(nw)
+        fail = p.output_data()["fail"]
+        w = torch.ones(32, 3, dtype=torch.float64, device="cuda")
+        out = torch.empty(32, NUM_THETA, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        p.adjoint_backward(w.data_ptr(), out.data_ptr())
+        g = out.cpu().numpy()
+    stopped = fail != 0
+    assert stopped.any() and (~stopped).any()
+    assert np.all(g[stopped] == 0.0)
+    assert np.all(np.isfinite(g[~stopped])) and np.any(g[~stopped] != 0.0)

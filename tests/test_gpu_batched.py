@@ -36,6 +36,9 @@ def sweep_sets(nsets=12, per=16):
                             E=(0.0, 0.0, 75e5 if r.uniform() < 0.5 else -75e5), diffuse=r.uniform(0.0, 0.5),
                             yi=(0.0, 0.0, 1.0), tf=tf, ioutInt=tf / 2, integratorType=0 if dop else 1, seed=s * per)
         sets.append(st.derive(o))
+    # a set without particles in the middle: it takes no work and no index
+    empty = st.make_options(numParticles=0, dist="M", T=0.4, gas_coll=True, tf=0.02, ioutInt=0.01, seed=99)
+    sets.insert(nsets // 2, st.derive(empty))
     return sets
 
 
@@ -62,6 +65,8 @@ def test_batched_sets_match_the_oracle_and_single_set_runs(gpu, oracle, kernel):
         n = int(o.numParticles)
         got = {k: v[first:first + n] for k, v in out.items()}
         first += n
+        if n == 0:
+            continue
         _, ref = oracle.run_sample(Options.from_buffer_copy(bytes(o)), 0, n)
         for f in ("fail", "n_coll", "n_bounce", "n_steps"):
             np.testing.assert_array_equal(got[f], ref[f], err_msg=f"set {s} {f}")
