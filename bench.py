@@ -140,6 +140,14 @@ def dist_setup():
     return world, rank, local
 
 
+def shard(n_total: int, world: int, rank: int) -> tuple[int, int]:
+    """Particles [first, first + n) of rank `rank`: equal shards, the last one
+    takes the remainder."""
+    per = n_total // world
+    first = rank * per
+    return first, (per if rank < world - 1 else n_total - first)
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -454,9 +462,7 @@ def run_ours(args, world, rank, local):
     dev = local
     torch.cuda.set_device(dev)
     n_total = args.particles
-    per = n_total // world
-    first = rank * per
-    n = per if rank < world - 1 else n_total - first
+    first, n = shard(n_total, world, rank)
     opt = workload_options(n, args.tf, first)
     nwin = st.num_windows(opt)
     sim = nwin * opt.ioutInt
