@@ -26,102 +26,7 @@
 namespace st {
 
 // ---------------------------------------------------------------- adjoint step
-namespace adj {
-// DOP853 stage structure as constexpr functions of compile-time stage and
-// term indices (they fold to constants inside the unrolled loops, so every
-// stage array stays in registers).
-// Earlier stages summed into stage s (2..12): stage 1, then 2 (s = 3),
-// 3.. (s = 4, 5) or 4.. (s >= 6).
-__device__ __forceinline__ constexpr int src(int s, int j) { return j == 0 ? 1 : (s == 3 ? 2 : (s <= 5 ? j + 2 : j + 3)); }
-__device__ __forceinline__ constexpr int cnt(int s) { return s <= 2 ? s - 1 : (s <= 4 ? 2 : (s == 5 ? 3 : s - 3)); }
-// coefficient of term j of stage s (the a_{s,src(s,j)} of the tableau)
-__device__ __forceinline__ constexpr double a(int s, int j) {
-  switch (s * 16 + j) {
-    case 32: return dop::A21;
-    case 48: return dop::A31;
-    case 49: return dop::A32;
-    case 64: return dop::A41;
-    case 65: return dop::A43;
-    case 80: return dop::A51;
-    case 81: return dop::A53;
-    case 82: return dop::A54;
-    case 96: return dop::A61;
-    case 97: return dop::A64;
-    case 98: return dop::A65;
-    case 112: return dop::A71;
-    case 113: return dop::A74;
-    case 114: return dop::A75;
-    case 115: return dop::A76;
-    case 128: return dop::A81;
-    case 129: return dop::A84;
-    case 130: return dop::A85;
-    case 131: return dop::A86;
-    case 132: return dop::A87;
-    case 144: return dop::A91;
-    case 145: return dop::A94;
-    case 146: return dop::A95;
-    case 147: return dop::A96;
-    case 148: return dop::A97;
-    case 149: return dop::A98;
-    case 160: return dop::A101;
-    case 161: return dop::A104;
-    case 162: return dop::A105;
-    case 163: return dop::A106;
-    case 164: return dop::A107;
-    case 165: return dop::A108;
-    case 166: return dop::A109;
-    case 176: return dop::A111;
-    case 177: return dop::A114;
-    case 178: return dop::A115;
-    case 179: return dop::A116;
-    case 180: return dop::A117;
-    case 181: return dop::A118;
-    case 182: return dop::A119;
-    case 183: return dop::A1110;
-    case 192: return dop::A121;
-    case 193: return dop::A124;
-    case 194: return dop::A125;
-    case 195: return dop::A126;
-    case 196: return dop::A127;
-    case 197: return dop::A128;
-    case 198: return dop::A129;
-    case 199: return dop::A1210;
-    case 200: return dop::A1211;
-    default: return 0.0;
-  }
-}
-// node of stage s (stage 12 at x + h)
-__device__ __forceinline__ constexpr double c(int s) {
-  switch (s) {
-    case 2: return dop::C2;
-    case 3: return dop::C3;
-    case 4: return dop::C4;
-    case 5: return dop::C5;
-    case 6: return dop::C6;
-    case 7: return dop::C7;
-    case 8: return dop::C8;
-    case 9: return dop::C9;
-    case 10: return dop::C10;
-    case 11: return dop::C11;
-    case 12: return 1.0;
-    default: return 0.0;
-  }
-}
-// 8th-order weight of stage s
-__device__ __forceinline__ constexpr double b(int s) {
-  switch (s) {
-    case 1: return dop::B1;
-    case 6: return dop::B6;
-    case 7: return dop::B7;
-    case 8: return dop::B8;
-    case 9: return dop::B9;
-    case 10: return dop::B10;
-    case 11: return dop::B11;
-    case 12: return dop::B12;
-    default: return 0.0;
-  }
-}
-}  // namespace adj
+// The stage structure (dopst::src, cnt, a, c, b) is shared with the forward stepper (st_device.cuh).
 
 struct Moments {
   double z0[3], z1[3], z2[3];
@@ -135,7 +40,7 @@ __device__ __forceinline__ void cross3(const double a[3], const double b[3], dou
 }
 
 __device__ __forceinline__ double stage_tau(int s, double tx, double h) {
-  return (s == 1) ? tx : (s == 12 ? tx + h : fma(adj::c(s), h, tx));
+  return (s == 1) ? tx : (s == 12 ? tx + h : fma(dopst::c(s), h, tx));
 }
 
 // Backward through one accepted DOP853 step from (x, y) with step h:
@@ -162,9 +67,9 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
       if (s == 1) {
         Y[c] = y[c];
       } else {
-        double acc = adj::a(s, 0) * K[adj::src(s, 0) - 1][c];
+        double acc = dopst::a(s, 0) * K[dopst::src(s, 0) - 1][c];
 #pragma unroll
-        for (int j = 1; j < adj::cnt(s); ++j) acc = fma(adj::a(s, j), K[adj::src(s, j) - 1][c], acc);
+        for (int j = 1; j < dopst::cnt(s); ++j) acc = fma(dopst::a(s, j), K[dopst::src(s, j) - 1][c], acc);
         Y[c] = fma(h, acc, y[c]);
       }
       ST_YS(s, c) = Y[c];
@@ -181,7 +86,7 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
 #pragma unroll
   for (int s = 1; s <= 12; ++s)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) kh[s - 1][c] = (adj::b(s) != 0.0) ? adj::b(s) * lam[c] : 0.0;
+    for (int c = 0; c < 3; ++c) kh[s - 1][c] = (dopst::b(s) != 0.0) ? dopst::b(s) * lam[c] : 0.0;
 #pragma unroll
   for (int s = 12; s >= 1; --s) {
     const double kb[3] = {h * kh[s - 1][0], h * kh[s - 1][1], h * kh[s - 1][2]};
@@ -207,10 +112,10 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
       M.gw = fma(-P.gamma * P.a * t * sn, z[2], M.gw);
     }
 #pragma unroll
-    for (int j = 0; j < adj::cnt(s); ++j) {
-      const int l = adj::src(s, j) - 1;
+    for (int j = 0; j < dopst::cnt(s); ++j) {
+      const int l = dopst::src(s, j) - 1;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) kh[l][c] = fma(adj::a(s, j), yb[c], kh[l][c]);
+      for (int c = 0; c < 3; ++c) kh[l][c] = fma(dopst::a(s, j), yb[c], kh[l][c]);
     }
   }
 #undef ST_YS

@@ -602,11 +602,123 @@ __device__ __forceinline__ void dop_begin(Seg& g, const SetParams& P, double Sx,
   feval(g, P, 0.0, Sx, Sy, Sz, g.kx, g.ky, g.kz);
 }
 
-// One attempted DOP853 step (one pass of the loop at src/integrator.cpp:128-247).
-// Returns 0 to continue, 1 when the segment's last step was accepted (g.h then
-// holds that step, as the reference returns it), -1 after more than nmax
-// attempts.
-__device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz) {
+// DOP853 stage structure as constexpr functions of compile-time stage and
+// term indices (they fold to constants inside unrolled loops).
+namespace dopst {
+// earlier stages summed into stage s (2..12): stage 1, then 2 (s = 3),
+// 3.. (s = 4, 5) or 4.. (s >= 6)
+__device__ __forceinline__ constexpr int src(int s, int j) { return j == 0 ? 1 : (s == 3 ? 2 : (s <= 5 ? j + 2 : j + 3)); }
+__device__ __forceinline__ constexpr int cnt(int s) { return s <= 2 ? s - 1 : (s <= 4 ? 2 : (s == 5 ? 3 : s - 3)); }
+// coefficient of term j of stage s (the a_{s,src(s,j)} of the tableau)
+__device__ __forceinline__ constexpr double a(int s, int j) {
+  switch (s * 16 + j) {
+    case 32: return dop::A21;
+    case 48: return dop::A31;
+    case 49: return dop::A32;
+    case 64: return dop::A41;
+    case 65: return dop::A43;
+    case 80: return dop::A51;
+    case 81: return dop::A53;
+    case 82: return dop::A54;
+    case 96: return dop::A61;
+    case 97: return dop::A64;
+    case 98: return dop::A65;
+    case 112: return dop::A71;
+    case 113: return dop::A74;
+    case 114: return dop::A75;
+    case 115: return dop::A76;
+    case 128: return dop::A81;
+    case 129: return dop::A84;
+    case 130: return dop::A85;
+    case 131: return dop::A86;
+    case 132: return dop::A87;
+    case 144: return dop::A91;
+    case 145: return dop::A94;
+    case 146: return dop::A95;
+    case 147: return dop::A96;
+    case 148: return dop::A97;
+    case 149: return dop::A98;
+    case 160: return dop::A101;
+    case 161: return dop::A104;
+    case 162: return dop::A105;
+    case 163: return dop::A106;
+    case 164: return dop::A107;
+    case 165: return dop::A108;
+    case 166: return dop::A109;
+    case 176: return dop::A111;
+    case 177: return dop::A114;
+    case 178: return dop::A115;
+    case 179: return dop::A116;
+    case 180: return dop::A117;
+    case 181: return dop::A118;
+    case 182: return dop::A119;
+    case 183: return dop::A1110;
+    case 192: return dop::A121;
+    case 193: return dop::A124;
+    case 194: return dop::A125;
+    case 195: return dop::A126;
+    case 196: return dop::A127;
+    case 197: return dop::A128;
+    case 198: return dop::A129;
+    case 199: return dop::A1210;
+    case 200: return dop::A1211;
+    default: return 0.0;
+  }
+}
+// node of stage s (stage 12 at x + h)
+__device__ __forceinline__ constexpr double c(int s) {
+  switch (s) {
+    case 2: return dop::C2;
+    case 3: return dop::C3;
+    case 4: return dop::C4;
+    case 5: return dop::C5;
+    case 6: return dop::C6;
+    case 7: return dop::C7;
+    case 8: return dop::C8;
+    case 9: return dop::C9;
+    case 10: return dop::C10;
+    case 11: return dop::C11;
+    case 12: return 1.0;
+    default: return 0.0;
+  }
+}
+// 8th-order weight of stage s
+__device__ __forceinline__ constexpr double b(int s) {
+  switch (s) {
+    case 1: return dop::B1;
+    case 6: return dop::B6;
+    case 7: return dop::B7;
+    case 8: return dop::B8;
+    case 9: return dop::B9;
+    case 10: return dop::B10;
+    case 11: return dop::B11;
+    case 12: return dop::B12;
+    default: return 0.0;
+  }
+}
+}  // namespace dopst
+
+// Where an attempt keeps its stage derivatives k2..k11 (k1 and k12 stay in
+// registers): registers (a local array that the unrolled code indexes with
+// constants), or this thread's column of a [10][3][BLOCK] shared-memory
+// array, which frees ~30 registers per thread.
+struct StageRegs {
+  double v[12][3];
+  __device__ __forceinline__ double& k(int s, int c) { return v[s][c]; }
+};
+struct StageSmem {
+  double* base;  // &array[0][0][thread]
+  int stride;    // BLOCK
+  __device__ __forceinline__ double& k(int s, int c) { return base[((s - 2) * 3 + c) * stride]; }
+};
+
+// One attempted DOP853 step (one pass of the loop at src/integrator.cpp:128-247),
+// stage derivatives in `ks`.  Returns 0 to continue, 1 when the segment's last
+// step was accepted (g.h then holds that step, as the reference returns it),
+// -1 after more than nmax attempts.
+template <class KS>
+__device__ __forceinline__ int dop_attempt_ks(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz,
+                                              KS& ks) {
   using namespace dop;
   if (g.nstep > P.nmax) return -1;
   double h = g.h;
@@ -619,61 +731,70 @@ __device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& S
   g.nstep++;
   g.acc = false;
   const double tx = g.x - g.t0;
-  const double k1x = g.kx, k1y = g.ky, k1z = g.kz;
-  double ax, ay, az, yx, yy, yz;
-#define ST_ACC1(c1, a) ax = (c1) * a##x; ay = (c1) * a##y; az = (c1) * a##z;
-#define ST_ACC(c, a) ax = fma((c), a##x, ax); ay = fma((c), a##y, ay); az = fma((c), a##z, az);
-#define ST_YY() yx = fma(h, ax, Sx); yy = fma(h, ay, Sy); yz = fma(h, az, Sz);
-  double k2x, k2y, k2z, k3x, k3y, k3z, k4x, k4y, k4z, k5x, k5y, k5z, k6x, k6y, k6z;
-  double k7x, k7y, k7z, k8x, k8y, k8z, k9x, k9y, k9z, k10x, k10y, k10z;
-  // stage 2
-  ST_ACC1(A21, k1) ST_YY() feval(g, P, fma(C2, h, tx), yx, yy, yz, k2x, k2y, k2z);
-  // stage 3
-  ST_ACC1(A31, k1) ST_ACC(A32, k2) ST_YY() feval(g, P, fma(C3, h, tx), yx, yy, yz, k3x, k3y, k3z);
-  // stage 4
-  ST_ACC1(A41, k1) ST_ACC(A43, k3) ST_YY() feval(g, P, fma(C4, h, tx), yx, yy, yz, k4x, k4y, k4z);
-  // stage 5
-  ST_ACC1(A51, k1) ST_ACC(A53, k3) ST_ACC(A54, k4) ST_YY() feval(g, P, fma(C5, h, tx), yx, yy, yz, k5x, k5y, k5z);
-  // stage 6
-  ST_ACC1(A61, k1) ST_ACC(A64, k4) ST_ACC(A65, k5) ST_YY() feval(g, P, fma(C6, h, tx), yx, yy, yz, k6x, k6y, k6z);
-  // stage 7
-  ST_ACC1(A71, k1) ST_ACC(A74, k4) ST_ACC(A75, k5) ST_ACC(A76, k6) ST_YY()
-  feval(g, P, fma(C7, h, tx), yx, yy, yz, k7x, k7y, k7z);
-  // stage 8
-  ST_ACC1(A81, k1) ST_ACC(A84, k4) ST_ACC(A85, k5) ST_ACC(A86, k6) ST_ACC(A87, k7) ST_YY()
-  feval(g, P, fma(C8, h, tx), yx, yy, yz, k8x, k8y, k8z);
-  // stage 9
-  ST_ACC1(A91, k1) ST_ACC(A94, k4) ST_ACC(A95, k5) ST_ACC(A96, k6) ST_ACC(A97, k7) ST_ACC(A98, k8) ST_YY()
-  feval(g, P, fma(C9, h, tx), yx, yy, yz, k9x, k9y, k9z);
-  // stage 10
-  ST_ACC1(A101, k1) ST_ACC(A104, k4) ST_ACC(A105, k5) ST_ACC(A106, k6) ST_ACC(A107, k7) ST_ACC(A108, k8)
-  ST_ACC(A109, k9) ST_YY()
-  feval(g, P, fma(C10, h, tx), yx, yy, yz, k10x, k10y, k10z);
-  // stage 11 (result in k2, which is no longer needed)
-  ST_ACC1(A111, k1) ST_ACC(A114, k4) ST_ACC(A115, k5) ST_ACC(A116, k6) ST_ACC(A117, k7) ST_ACC(A118, k8)
-  ST_ACC(A119, k9) ST_ACC(A1110, k10) ST_YY()
-  feval(g, P, fma(C11, h, tx), yx, yy, yz, k2x, k2y, k2z);
-  // stage 12 at x + h (result in k3); its Omega is reused for the FSAL derivative
-  ST_ACC1(A121, k1) ST_ACC(A124, k4) ST_ACC(A125, k5) ST_ACC(A126, k6) ST_ACC(A127, k7) ST_ACC(A128, k8)
-  ST_ACC(A129, k9) ST_ACC(A1210, k10) ST_ACC(A1211, k2) ST_YY()
+  const double S0[3] = {Sx, Sy, Sz};
+  const double k1[3] = {g.kx, g.ky, g.kz};
+  // stages 2..11: y + h * sum_j a_sj k_j, then k_s = f(x + c_s h, .)
+#pragma unroll
+  for (int s = 2; s <= 11; ++s) {
+    double Y[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double acc = dopst::a(s, 0) * k1[c];
+#pragma unroll
+      for (int j = 1; j < dopst::cnt(s); ++j) acc = fma(dopst::a(s, j), ks.k(dopst::src(s, j), c), acc);
+      Y[c] = fma(h, acc, S0[c]);
+    }
+    double kx, ky, kz;
+    feval(g, P, fma(dopst::c(s), h, tx), Y[0], Y[1], Y[2], kx, ky, kz);
+    ks.k(s, 0) = kx;
+    ks.k(s, 1) = ky;
+    ks.k(s, 2) = kz;
+  }
+  // stage 12 at x + h; its Omega is reused for the FSAL derivative
+  double Y12[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double acc = dopst::a(12, 0) * k1[c];
+#pragma unroll
+    for (int j = 1; j < dopst::cnt(12); ++j) acc = fma(dopst::a(12, j), ks.k(dopst::src(12, j), c), acc);
+    Y12[c] = fma(h, acc, S0[c]);
+  }
   const double tph = tx + h;
-  double Ox12, Oy12, Oz12;
+  double Ox12, Oy12, Oz12, k12[3];
   omega_at(g, P, tph, Ox12, Oy12, Oz12);
-  bloch(yx, yy, yz, Ox12, Oy12, Oz12, k3x, k3y, k3z);
+  bloch(Y12[0], Y12[1], Y12[2], Ox12, Oy12, Oz12, k12[0], k12[1], k12[2]);
   // 8th-order combination and the new state
-  ST_ACC1(B1, k1) ST_ACC(B6, k6) ST_ACC(B7, k7) ST_ACC(B8, k8) ST_ACC(B9, k9) ST_ACC(B10, k10) ST_ACC(B11, k2)
-  ST_ACC(B12, k3)
-  const double bx = ax, by = ay, bz = az;
+  double bsum[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double acc = B1 * k1[c];
+    acc = fma(B6, ks.k(6, c), acc);
+    acc = fma(B7, ks.k(7, c), acc);
+    acc = fma(B8, ks.k(8, c), acc);
+    acc = fma(B9, ks.k(9, c), acc);
+    acc = fma(B10, ks.k(10, c), acc);
+    acc = fma(B11, ks.k(11, c), acc);
+    bsum[c] = fma(B12, k12[c], acc);
+  }
+  const double bx = bsum[0], by = bsum[1], bz = bsum[2];
   const double nx = fma(h, bx, Sx), ny = fma(h, by, Sy), nz = fma(h, bz, Sz);
   // error estimates: 3rd-order (bhh) and 5th-order (er) rows
-  const double e1x = fma(-BHH3, k3x, fma(-BHH2, k9x, fma(-BHH1, k1x, bx)));
-  const double e1y = fma(-BHH3, k3y, fma(-BHH2, k9y, fma(-BHH1, k1y, by)));
-  const double e1z = fma(-BHH3, k3z, fma(-BHH2, k9z, fma(-BHH1, k1z, bz)));
-  ST_ACC1(ER1, k1) ST_ACC(ER6, k6) ST_ACC(ER7, k7) ST_ACC(ER8, k8) ST_ACC(ER9, k9) ST_ACC(ER10, k10) ST_ACC(ER11, k2)
-  ST_ACC(ER12, k3)
-#undef ST_ACC1
-#undef ST_ACC
-#undef ST_YY
+  const double e1x = fma(-BHH3, k12[0], fma(-BHH2, ks.k(9, 0), fma(-BHH1, k1[0], bx)));
+  const double e1y = fma(-BHH3, k12[1], fma(-BHH2, ks.k(9, 1), fma(-BHH1, k1[1], by)));
+  const double e1z = fma(-BHH3, k12[2], fma(-BHH2, ks.k(9, 2), fma(-BHH1, k1[2], bz)));
+  double er[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double acc = ER1 * k1[c];
+    acc = fma(ER6, ks.k(6, c), acc);
+    acc = fma(ER7, ks.k(7, c), acc);
+    acc = fma(ER8, ks.k(8, c), acc);
+    acc = fma(ER9, ks.k(9, c), acc);
+    acc = fma(ER10, ks.k(10, c), acc);
+    acc = fma(ER11, ks.k(11, c), acc);
+    er[c] = fma(ER12, k12[c], acc);
+  }
+  const double ax = er[0], ay = er[1], az = er[2];
   const double wx = rcp_full(fma(P.rtol, max_d(fabs(Sx), fabs(nx)), P.atol));
   const double wy = rcp_full(fma(P.rtol, max_d(fabs(Sy), fabs(ny)), P.atol));
   const double wz = rcp_full(fma(P.rtol, max_d(fabs(Sz), fabs(nz)), P.atol));
@@ -721,6 +842,13 @@ __device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& S
   g.last = last;
   g.h = P.fixed ? h : hnew;
   return ret;
+}
+
+
+// One attempted DOP853 step with the stage derivatives in registers.
+__device__ __forceinline__ int dop_attempt(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz) {
+  StageRegs ks;
+  return dop_attempt_ks(g, P, Sx, Sy, Sz, ks);
 }
 
 // ------------------------------------------------------------ RK45

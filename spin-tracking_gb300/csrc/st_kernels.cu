@@ -6,14 +6,16 @@
 //                particle to the window end with the reference's nested loops
 //                (segment loop, step loop), one launch per output window
 //                (src/particle.cpp:525-635, 865-876).
-//  k_persistent  the batched engine: a persistent grid whose lanes pull
+//  k_persistent  the flattened engine: a persistent grid whose lanes pull
 //                particles (of any parameter set) from a device work queue and
-//                run them through all requested windows.  The per-lane loop is
-//                flattened so that every iteration performs exactly one step
-//                attempt: a lane whose segment ended does its trajectory event
-//                and joins the next attempt, and a lane whose particle finished
-//                takes the next particle, so warps stay converged on the step
-//                code.  Snapshots go straight to the snapshot buffer.
+//                run them through all requested windows; every iteration of a
+//                lane's loop is one step attempt (a lane whose segment ended
+//                does its trajectory event inline and rejoins).
+//  k_batched     the trajectory-ahead engine (the default): as k_persistent,
+//                but each lane keeps a shared-memory ring of upcoming segments,
+//                produced warp-synchronously ahead of the spin, so the step loop
+//                rarely leaves the converged path.  Template switches: the
+//                adjoint's tape, gas collisions, stage storage.
 //  k_pack        copies the state into one snapshot block (plain path).
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -438,12 +440,15 @@ enum BatchedMode { B_FETCH = 0, B_NEED = 1, B_SEG = 2, B_WEND = 3, B_DONE = 4 };
 // TAPE: also write the adjoint tape (steps and segments of every particle)
 // and state checkpoints at every ta.ckpt_every-th window end.
 // GAS = false: the instantiation for launches without gas collisions.
-template <int BLOCK, int MINB, int QCAP, bool TAPE, bool GAS>
+// STAGES = 1: DOP853 stage derivatives k2..k11 in shared memory (after the
+// rings), not in registers.
+template <int BLOCK, int MINB, int QCAP, bool TAPE, bool GAS, int STAGES>
 __global__ void __launch_bounds__(BLOCK, MINB)
     k_batched(RunArgs a, int topup_start, int topup_keep, int defer_k, TapeArgs ta) {
   extern __shared__ double st_smem[];
   double* qd = st_smem;
   int* qf = reinterpret_cast<int*>(st_smem + (size_t)QCAP * kRecF * BLOCK);
+  double* stage_col = st_smem + (size_t)QCAP * kRecF * BLOCK + (size_t)(QCAP * BLOCK + 1) / 2 + threadIdx.x;
   const int tid = threadIdx.x;
   const unsigned FULL = 0xffffffffu;
   int mode = B_FETCH;
@@ -614,7 +619,12 @@ __global__ void __launch_bounds__(BLOCK, MINB)
       int r;
       if (P->integrator == 0) {
         const double y0x = tp.Sx, y0y = tp.Sy, y0z = tp.Sz, x0 = g.x;
-        r = dop_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
+        if (STAGES) {
+          StageSmem ks{stage_col, BLOCK};
+          r = dop_attempt_ks(g, *P, tp.Sx, tp.Sy, tp.Sz, ks);
+        } else {
+          r = dop_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
+        }
         ++n_dop;
         if (TAPE && g.acc) tape_step(ta, tc, y0x, y0y, y0z, x0, g.hu);
       } else {
@@ -740,16 +750,18 @@ int launch_pack_snapshot(const RunArgs& a, int slot, void* stream) {
 // while this many still have room).  Block threads and the minimum resident
 // blocks per SM set the register budget.
 struct Variant {
-  int family, block, minb, qcap, tstart, tkeep, defer;
+  int family, block, minb, qcap, tstart, tkeep, defer, stages;
   const char* name;
 };
 static const Variant kVariants[] = {
-    {0, 128, 1, 0, 0, 0, 0, "flat_b128_m1"},  {0, 128, 2, 0, 0, 0, 0, "flat_b128_m2"},
-    {0, 128, 3, 0, 0, 0, 0, "flat_b128_m3"},  {0, 64, 4, 0, 0, 0, 0, "flat_b64_m4"},
-    {0, 256, 1, 0, 0, 0, 0, "flat_b256_m1"},  {1, 128, 1, 6, 24, 16, 12, "ahead_b128_q6_t24_d12"},
-    {1, 128, 1, 6, 16, 12, 12, "ahead_b128_q6_t16_d12"}, {1, 128, 2, 4, 24, 16, 12, "ahead_b128_q4_t24_d12"},
-    {1, 64, 2, 8, 24, 16, 12, "ahead_b64_q8_t24_d12"},   {1, 64, 2, 8, 24, 16, 6, "ahead_b64_q8_t24_d6"},
-    {1, 64, 2, 8, 24, 16, 18, "ahead_b64_q8_t24_d18"},   {1, 64, 2, 8, 28, 20, 12, "ahead_b64_q8_t28_d12"},
+    {0, 128, 1, 0, 0, 0, 0, 0, "flat_b128_m1"},  {0, 128, 2, 0, 0, 0, 0, 0, "flat_b128_m2"},
+    {0, 128, 3, 0, 0, 0, 0, 0, "flat_b128_m3"},  {0, 64, 4, 0, 0, 0, 0, 0, "flat_b64_m4"},
+    {0, 256, 1, 0, 0, 0, 0, 0, "flat_b256_m1"},  {1, 128, 1, 6, 24, 16, 12, 0, "ahead_b128_q6_t24_d12"},
+    {1, 128, 1, 6, 16, 12, 12, 0, "ahead_b128_q6_t16_d12"}, {1, 128, 2, 4, 24, 16, 12, 0, "ahead_b128_q4_t24_d12"},
+    {1, 64, 2, 8, 24, 16, 12, 0, "ahead_b64_q8_t24_d12"},   {1, 64, 2, 8, 24, 16, 6, 0, "ahead_b64_q8_t24_d6"},
+    {1, 64, 2, 8, 24, 16, 18, 0, "ahead_b64_q8_t24_d18"},   {1, 64, 2, 8, 28, 20, 12, 0, "ahead_b64_q8_t28_d12"},
+    {1, 64, 2, 8, 28, 20, 12, 1, "ahead_b64_q8_t28_d12_ksmem"},
+    {1, 64, 5, 6, 28, 20, 12, 1, "ahead_b64_m5_q6_t28_d12_ksmem"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -766,17 +778,26 @@ static const void* variant_fn_g(int v) {
     case 3: return reinterpret_cast<const void*>(&k_persistent<64, 4>);
     case 4: return reinterpret_cast<const void*>(&k_persistent<256, 1>);
     case 5:
-    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, GAS>);
-    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, GAS>);
-    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS>);  // 8 and up
+    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, GAS, 0>);
+    case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, GAS, 0>);
+    case 12: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 1>);
+    case 13: return reinterpret_cast<const void*>(&k_batched<64, 5, 6, false, GAS, 1>);
+    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 0>);  // 8 to 11
   }
 }
 static const void* variant_fn(int v, bool gas) { return gas ? variant_fn_g<true>(v) : variant_fn_g<false>(v); }
 
+// Rings (records and flags), then the stage derivatives when they live in
+// shared memory (10 stages x 3 components x block).
+static size_t batched_smem(int block, int qcap, int stages) {
+  const size_t ring = (size_t)qcap * block * kRecF * sizeof(double) + (size_t)(qcap * block + 1) / 2 * sizeof(double);
+  return ring + (stages ? (size_t)30 * block * sizeof(double) : 0);
+}
+
 static size_t variant_smem(int v) {
   const Variant& x = kVariants[v];
   if (x.family == 0) return 0;
-  return (size_t)x.qcap * x.block * (kRecF * sizeof(double) + sizeof(int));
+  return batched_smem(x.block, x.qcap, x.stages);
 }
 
 // Opt the kernels that need more than 48 KiB of dynamic shared memory in, once.
@@ -830,10 +851,10 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
 // (one configuration: 128 lanes, 6-record rings, top-up at 24 / 16 lanes).
 constexpr int kTapeBlock = 128, kTapeQcap = 6;
 static const void* tape_fn(bool gas) {
-  return gas ? reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, true>)
-             : reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, false>);
+  return gas ? reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, true, 0>)
+             : reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, false, 0>);
 }
-static size_t tape_smem() { return (size_t)kTapeQcap * kTapeBlock * (kRecF * sizeof(double) + sizeof(int)); }
+static size_t tape_smem() { return batched_smem(kTapeBlock, kTapeQcap, 0); }
 
 static cudaError_t tape_ensure_smem(bool gas) {
   static bool done[2] = {};
