@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
         if (pm == 0u || __popc(pm) < topup_keep) break;
       }
       if (starved_m != 0u) {
-        // a starved lane always gets a record in round 0; this bound only
+        // a starved lane always gets a record in the first top-up pass; this bound only
         // protects the device from a logic error
         if (++dry > 1000000u) {
           hit = true;
