@@ -128,8 +128,9 @@ int st_run_until(st_ctx *ctx, double next_t);
 int st_run_windows(st_ctx *ctx, int kernel, int w_begin, int w_end, void *snap);
 /* Bytes of one device snapshot block and the offset of field f within it
  * (f: 0 t, 1 pos_x, 2 pos_y, 3 pos_z, 4 v_x, 5 v_y, 6 v_z, 7 S_x, 8 S_y,
- * 9 S_z, 10 fail(i32), 11 n_coll, 12 n_bounce, 13 n_steps; each field an
- * array over all particles, 256-byte aligned). */
+ * 9 S_z, 10 fail(i32), 11 n_coll, 12 n_bounce, 13 n_steps, 14 precession
+ * turns (i32, see st_gather_phase); each field an array over all particles,
+ * 256-byte aligned). */
 size_t st_snapshot_bytes(const st_ctx *ctx);
 size_t st_snapshot_field_offset(const st_ctx *ctx, int field);
 /* particle::outputData, src/particle.cpp:852-862: synchronise and copy the
@@ -185,7 +186,7 @@ int st_get_counters(const st_ctx *ctx, st_counters *out);
  * library until the process exits.  It calls no cudaMalloc/cudaFree.
  *   state == NULL: writes the required buffer size to *state_bytes, returns.
  *   state != NULL: a 256-byte aligned device buffer of *state_bytes bytes;
- *     on return it holds the particle state after window w_end as 27 arrays
+ *     on return it holds the particle state after window w_end as 28 arrays
  *     over all particles (sets in order), each starting on a 256-byte
  *     boundary: t, pos_x, pos_y, pos_z, v_x, v_y, v_z, S_x, S_y, S_z (f64),
  *     fail (i32), n_coll, n_bounce, n_steps (u64), then internal fields.
@@ -239,6 +240,15 @@ typedef struct {
 } st_adjoint_stats;
 int st_adjoint_get_stats(const st_ctx *ctx, st_adjoint_stats *out);
 
+/* Unwrapped precession phase of every particle about x, accumulated on the
+ * device over the whole run: atan2(Sz, Sy) + 2 pi * turns, where turns counts
+ * the accepted steps that carried the spin's (y, z) projection across the
+ * cut at +-pi (Sz changing sign with Sy < 0; a step at rtol 1e-12 turns the
+ * spin by far less than pi).  Unlike phases taken from snapshots, it stays
+ * continuous however long the window.  dst: device array, one double per
+ * particle.  No counterpart in the reference (its scripts wrap phases). */
+int st_gather_phase(st_ctx *ctx, double *dst);
+
 /* ---- ensemble statistics (on the device) ------------------------------ */
 /* The reference computes these in its analysis scripts from the output file
  * (scripts/nedmSim.py:151-179 shiftDatapoints,
@@ -263,6 +273,12 @@ typedef struct {
   double phase_expected;
   double freq_shift;      /* Hz */
   double freq_shift_err;  /* phase_stderr / (2 pi t), Hz */
+  /* the unwrapped phase (st_gather_phase) over the counted particles: mean,
+   * population std, and its shift against the continuous expected phase
+   * phi0 - w t (phi0 = atan2(yi_z, yi_y)), in Hz: no +-pi ambiguity */
+  double phase_unwrapped_mean;
+  double phase_unwrapped_std;
+  double freq_shift_unwrapped;
 } st_ensemble;
 /* snap: a device snapshot block (st_snapshot_bytes) or NULL for the current
  * state; set: parameter-set index. */

@@ -222,7 +222,7 @@ size_t state_layout(st::DeviceState& s, char* base, int64_t n) {
                {(void**)&s.rx, 8},       {(void**)&s.ry, 8},   {(void**)&s.rz, 8},     {(void**)&s.rw, 8},
                {(void**)&s.rspare, 8},   {(void**)&s.rhas, 1}, {(void**)&s.fail, 4},   {(void**)&s.n_coll, 8},
                {(void**)&s.n_bounce, 8}, {(void**)&s.n_steps, 8}, {(void**)&s.stop, 1}, {(void**)&s.coll, 1},
-               {(void**)&s.wall, 1},     {(void**)&s.set, 4},  {(void**)&s.w_done, 4}};
+               {(void**)&s.wall, 1},     {(void**)&s.set, 4},  {(void**)&s.w_done, 4},  {(void**)&s.turns, 4}};
   size_t off = 0;
   for (auto& x : f) {
     *x.ptr = base ? base + off : nullptr;
@@ -256,11 +256,11 @@ int ctx_alloc(st_ctx* c) {
   ST_CUDA(cudaMalloc(&c->status_d, sizeof(st::RunStatus)));
   ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
   ST_CUDA(cudaMallocHost(&c->status_h, sizeof(st::RunStatus)));
-  // snapshot block layout: 14 arrays of n entries
-  const size_t esz[14] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 4, 8, 8, 8};
+  // snapshot block layout: kSnapFields arrays of n entries
+  const size_t esz[st::kSnapFields] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 4, 8, 8, 8, 4};
   size_t off = 0;
   c->snap.n = n;
-  for (int k = 0; k < 14; ++k) {
+  for (int k = 0; k < st::kSnapFields; ++k) {
     c->snap.off[k] = off;
     off += align256(esz[k] * m);
   }
@@ -721,7 +721,9 @@ int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
 }
 
 size_t st_snapshot_bytes(const st_ctx* c) { return c ? c->snap.bytes : 0; }
-size_t st_snapshot_field_offset(const st_ctx* c, int f) { return (c && f >= 0 && f < 14) ? c->snap.off[f] : 0; }
+size_t st_snapshot_field_offset(const st_ctx* c, int f) {
+  return (c && f >= 0 && f < st::kSnapFields) ? c->snap.off[f] : 0;
+}
 
 int st_read_state(st_ctx* c, const st_state_view* h) {
   if (!c || !h) return fail(ST_ERR_ARG, "null argument");
@@ -763,6 +765,15 @@ int st_gather_spins(st_ctx* c, double* dst) {
   for (int k = 0; k < 3; ++k)
     ST_CUDA(cudaMemcpy2DAsync(dst + k, 3 * sizeof(double), src[k], sizeof(double), sizeof(double), (size_t)c->n,
                               cudaMemcpyDeviceToDevice, c->stream));
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  return ST_OK;
+}
+
+int st_gather_phase(st_ctx* c, double* dst) {
+  if (!c || !dst) return fail(ST_ERR_ARG, "null argument");
+  ST_CUDA(cudaSetDevice(c->device));
+  int e = st::launch_gather_phase(c->s.Sy, c->s.Sz, c->s.turns, c->n, dst, c->stream);
+  if (e) return fail(ST_ERR_CUDA, std::string("phase launch: ") + cudaGetErrorString((cudaError_t)e));
   ST_CUDA(cudaStreamSynchronize(c->stream));
   return ST_OK;
 }
@@ -1245,7 +1256,7 @@ int st_ensemble_stats(st_ctx* c, const void* snap, int set, st_ensemble* out) {
   double* part = (double*)((char*)c->ens_buf + ctl_b);
   unsigned int* hist = (unsigned int*)((char*)c->ens_buf + ctl_b + part_b);
   const double *t, *sx, *sy, *sz;
-  const int32_t* fl;
+  const int32_t *fl, *tn;
   if (snap) {
     const char* b = (const char*)snap;
     t = (const double*)(b + c->snap.off[0]);
@@ -1253,15 +1264,17 @@ int st_ensemble_stats(st_ctx* c, const void* snap, int set, st_ensemble* out) {
     sy = (const double*)(b + c->snap.off[8]);
     sz = (const double*)(b + c->snap.off[9]);
     fl = (const int32_t*)(b + c->snap.off[10]);
+    tn = (const int32_t*)(b + c->snap.off[14]);
   } else {
     t = c->s.t;
     sx = c->s.Sx;
     sy = c->s.Sy;
     sz = c->s.Sz;
     fl = c->s.fail;
+    tn = c->s.turns;
   }
   const SetParams& P = c->sets_h[(size_t)set];
-  int e = st::ensemble_device(t, sx, sy, sz, fl, P.first, P.n, ctl, part, hist, st::kEnsMaxBlocks, c->stream);
+  int e = st::ensemble_device(t, sx, sy, sz, fl, tn, P.first, P.n, ctl, part, hist, st::kEnsMaxBlocks, c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("ensemble launch: ") + cudaGetErrorString((cudaError_t)e));
   double h[32];
   ST_CUDA(cudaMemcpyAsync(h, ctl, sizeof(double) * st::ensemble_ctl_count(), cudaMemcpyDeviceToHost, c->stream));
@@ -1290,6 +1303,10 @@ int st_ensemble_stats(st_ctx* c, const void* snap, int set, st_ensemble* out) {
   if (shift < -pi) shift += 2.0 * pi;
   r.freq_shift = shift / r.t / (2.0 * pi);
   r.freq_shift_err = r.phase_stderr / r.t / (2.0 * pi);
+  r.phase_unwrapped_mean = h[st::ENS_UMEAN];
+  r.phase_unwrapped_std = h[st::ENS_USTD];
+  const double phi0 = std::atan2(P.yi_z, P.yi_y);
+  r.freq_shift_unwrapped = (r.phase_unwrapped_mean - (phi0 - w * r.t)) / r.t / (2.0 * pi);
   *out = r;
   return ST_OK;
 }

@@ -153,6 +153,7 @@ struct PState {
   Rng rng;
   uint64_t n_coll, n_bounce, n_steps;
   int fail;
+  int turns;  // precession turns about x (see count_turn)
   bool stop;
   char coll, wall;
 };
@@ -170,6 +171,7 @@ __device__ __forceinline__ PState load_state(const DeviceState& s, int64_t i) {
   p.rng.has = s.rhas[i] != 0;
   p.n_coll = s.n_coll[i]; p.n_bounce = s.n_bounce[i]; p.n_steps = s.n_steps[i];
   p.fail = s.fail[i];
+  p.turns = s.turns[i];
   p.stop = s.stop[i] != 0;
   p.coll = (char)s.coll[i];
   p.wall = (char)s.wall[i];
@@ -188,6 +190,7 @@ __device__ __forceinline__ void store_state(const DeviceState& s, int64_t i, con
   s.rhas[i] = p.rng.has ? 1 : 0;
   s.n_coll[i] = p.n_coll; s.n_bounce[i] = p.n_bounce; s.n_steps[i] = p.n_steps;
   s.fail[i] = p.fail;
+  s.turns[i] = p.turns;
   s.stop[i] = p.stop ? 1 : 0;
   s.coll[i] = (uint8_t)p.coll;
   s.wall[i] = (uint8_t)p.wall;
@@ -224,6 +227,7 @@ __device__ inline PState init_particle(const SetParams& P, unsigned int ipart) {
   p.coll = 'W';
   p.wall = 0;
   p.fail = 0;
+  p.turns = 0;
   p.n_coll = p.n_bounce = p.n_steps = 0;
   return p;
 }
@@ -481,9 +485,22 @@ struct Seg {
   double lastH, lnprev;
   double hu;           // step size of the last accepted attempt (read by the adjoint replay)
   unsigned int nstep;
+  int turns;           // precession turns of the segment's accepted steps (count_turn)
   bool reject, last;
   bool acc;            // the last attempt was accepted
 };
+
+// Precession phase accumulation: the phase phi = atan2(Sz, Sy) about x jumps
+// by 2 pi where the spin's (y, z) projection crosses the cut at phi = +-pi
+// (Sy < 0, Sz changing sign).  An accepted step at rtol 1e-12 turns the spin
+// by far less than pi, so a crossing is a sign change of Sz with Sy < 0 at
+// both ends, counted +1 from phi near +pi to near -pi (phi increasing) and -1
+// back; atan2(Sz, Sy) + 2 pi * turns is then continuous along the run.
+__device__ __forceinline__ int count_turn(double y0, double z0, double y1, double z1) {
+  if (!(y0 < 0.0 && y1 < 0.0)) return 0;
+  const bool s0 = signbit(z0), s1 = signbit(z1);
+  return (s0 == s1) ? 0 : (s1 ? 1 : -1);
+}
 
 // The per-set field constants (launch_prepare_sets): gamma * B0, the gradient
 // tensor's columns through the st_grad hook, gamma * E / c^2 and the gravity
@@ -597,6 +614,7 @@ __device__ __forceinline__ void dop_begin(Seg& g, const SetParams& P, double Sx,
   g.h = h;
   g.facold = 1.0e-4;
   g.nstep = 0;
+  g.turns = 0;
   g.reject = false;
   g.last = false;
   feval(g, P, 0.0, Sx, Sy, Sz, g.kx, g.ky, g.kz);
@@ -824,6 +842,7 @@ __device__ __forceinline__ int dop_attempt_ks(Seg& g, const SetParams& P, double
     g.hu = h;
     g.facold = max_d(err, 1.0e-4);
     bloch(nx, ny, nz, Ox12, Oy12, Oz12, g.kx, g.ky, g.kz);  // FSAL: f(x + h, y_new)
+    g.turns += count_turn(Sy, Sz, ny, nz);
     Sx = nx; Sy = ny; Sz = nz;
     g.x = g.x + h;
     if (last) {
@@ -858,6 +877,7 @@ __device__ __forceinline__ void rk45_begin(Seg& g, double h) {
   g.lnprev = 0.0;  // log(prev_ratio = 1)
   g.kx = g.ky = g.kz = 0.0;  // the stage state a fresh call starts from
   g.nstep = 0;
+  g.turns = 0;
   g.last = false;
 }
 
@@ -926,7 +946,9 @@ __device__ __forceinline__ int rk45_attempt(Seg& g, const SetParams& P, double& 
   double q = exp(E1 * lnr + E2 * g.lnprev);  // ratio^E1 * prev_ratio^E2
   q = std_min(q, 4.0);
   if ((q > 0.81 && error < 2.0 * P.rtol) || P.fixed) {
-    Sx = fma(h, wx, Sx); Sy = fma(h, wy, Sy); Sz = fma(h, wz, Sz);
+    const double ny = fma(h, wy, Sy), nz = fma(h, wz, Sz);
+    g.turns += count_turn(Sy, Sz, ny, nz);
+    Sx = fma(h, wx, Sx); Sy = ny; Sz = nz;
     g.x += h;
     if (stop) {
       g.h = g.lastH;

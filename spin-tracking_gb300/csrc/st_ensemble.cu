@@ -10,6 +10,8 @@
 //   mean and population std of what is left, the mean wrapped to [-pi, pi];
 //   frequency shift = wrap(mean - atan2(cos(w t), sin(w t))) / (2 pi t),
 //          w = gamma |B0| sign(B0x).
+// Also the mean and population std of the unwrapped phase atan2(Sz, Sy) +
+// 2 pi turns over the same particles (no alignment needed).
 // Sums are per-block partials combined by one thread in block order, so the
 // result is the same on every call.
 #include <cuda_runtime.h>
@@ -29,9 +31,11 @@ constexpr double kPi = 3.141592653589793;
 
 struct EnsView {
   const double *t, *Sx, *Sy, *Sz;
-  const int32_t* fail;
+  const int32_t *fail, *turns;
   int64_t first, n;
 };
+
+__device__ __forceinline__ double unwrapped(double phi, int turns) { return fma(2.0 * kPi, (double)turns, phi); }
 
 // ctl slots: the ENS_* indices of st_internal.h
 
@@ -109,6 +113,15 @@ __global__ void __launch_bounds__(kEnsBlock) k_ens_pass(EnsView v, int pass, con
       acc[5] = fmax(acc[5], phi);
     } else if (pass == 1) {
       atomicAdd(&hsh[ens_bin(phi, ctl[ENS_EDGE0], ctl[ENS_EDGE1])], 1u);
+    } else if (pass >= 6) {  // unwrapped phase: sum, then squared deviations
+      const double u = unwrapped(phi, v.turns[i]);
+      if (pass == 6) {
+        acc[0] += 1.0;
+        acc[1] += u;
+      } else {
+        const double d = u - ctl[ENS_UMEAN];
+        acc[1] = fma(d, d, acc[1]);
+      }
     } else {
       const double p = ens_align(phi, ctl[ENS_LOC]);
       if (pass >= 4) {  // numpy: shifted < mean - std * 5, shifted > mean + std * 5
@@ -188,8 +201,12 @@ __global__ void k_ens_finish(EnsView v, int pass, double* ctl, const double* par
     } else if (pass == 4) {
       ctl[ENS_KEPT] = c;
       ctl[ENS_MEAN2] = s / c;
-    } else {
+    } else if (pass == 5) {
       ctl[ENS_STD2] = sqrt(s / ctl[ENS_KEPT]);
+    } else if (pass == 6) {
+      ctl[ENS_UMEAN] = s / c;
+    } else {
+      ctl[ENS_USTD] = sqrt(s / ctl[ENS_COUNT]);
     }
   }
 }
@@ -198,20 +215,35 @@ __global__ void k_ens_finish(EnsView v, int pass, double* ctl, const double* par
 // Run the passes for particles [first, first + n) of the given arrays; ctl
 // receives ensemble_ctl_count() doubles (slots of the enum above).
 int ensemble_device(const double* t, const double* Sx, const double* Sy, const double* Sz, const int32_t* fail,
-                    int64_t first, int64_t n, double* ctl, double* part, unsigned int* hist, int max_blocks,
-                    void* stream) {
+                    const int32_t* turns, int64_t first, int64_t n, double* ctl, double* part, unsigned int* hist,
+                    int max_blocks, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
-  EnsView v{t, Sx, Sy, Sz, fail, first, n};
+  EnsView v{t, Sx, Sy, Sz, fail, turns, first, n};
   const int nblk = (int)std::min<int64_t>(max_blocks, std::max<int64_t>(1, (n + kEnsBlock - 1) / kEnsBlock));
   cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * kEnsBins, s);
   if (e != cudaSuccess) return (int)e;
-  for (int pass = 0; pass <= 5; ++pass) {
+  for (int pass = 0; pass <= 7; ++pass) {
     k_ens_pass<<<nblk, kEnsBlock, 0, s>>>(v, pass, ctl, part, hist);
     k_ens_finish<<<1, 32, 0, s>>>(v, pass, ctl, part, nblk, hist);
   }
   return (int)cudaGetLastError();
 }
 
-int ensemble_ctl_count() { return ENS_KEPT + 1; }
+int ensemble_ctl_count() { return ENS_USTD + 1; }
+
+// ---------------------------------------------------------------- phase
+namespace {
+__global__ void k_gather_phase(const double* Sy, const double* Sz, const int32_t* turns, int64_t n, double* dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = unwrapped(atan2(Sz[i], Sy[i]), turns[i]);
+}
+}  // namespace
+
+int launch_gather_phase(const double* Sy, const double* Sz, const int32_t* turns, int64_t n, double* dst,
+                        void* stream) {
+  if (n <= 0) return 0;
+  k_gather_phase<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(Sy, Sz, turns, n, dst);
+  return (int)cudaGetLastError();
+}
 
 }  // namespace st

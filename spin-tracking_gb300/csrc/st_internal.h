@@ -61,12 +61,15 @@ struct DeviceState {
   uint8_t *stop, *coll, *wall;
   int32_t *set;                   // parameter set of each particle
   int32_t *w_done;                // windows completed
+  int32_t *turns;                 // precession turns: unwrapped phase = atan2(Sz, Sy) + 2 pi turns
 };
 
-// Snapshot block: 14 field arrays over all particles, each padded to 256 B.
+// Snapshot block: 15 field arrays over all particles (the 14 of the state
+// view, then the precession turns), each padded to 256 B.
+constexpr int kSnapFields = 15;
 struct SnapLayout {
   int64_t n;
-  size_t off[14];
+  size_t off[kSnapFields];
   size_t bytes;
 };
 
@@ -148,12 +151,15 @@ int adj_backward_max_blocks_per_sm();
 
 // Ensemble statistics (st_ensemble.cu).
 int ensemble_device(const double* t, const double* Sx, const double* Sy, const double* Sz, const int32_t* fail,
-                    int64_t first, int64_t n, double* ctl, double* part, unsigned int* hist, int max_blocks,
-                    void* stream);
+                    const int32_t* turns, int64_t first, int64_t n, double* ctl, double* part, unsigned int* hist,
+                    int max_blocks, void* stream);
 int ensemble_ctl_count();
 constexpr int kEnsMaxBlocks = 1024, kEnsHistBins = 1000;
 enum { ENS_COUNT = 0, ENS_SX, ENS_SY, ENS_SZ, ENS_MIN, ENS_MAX, ENS_T, ENS_EDGE0, ENS_EDGE1, ENS_LOC, ENS_MEAN1,
-       ENS_STD1, ENS_MEAN2, ENS_STD2, ENS_KEPT };
+       ENS_STD1, ENS_MEAN2, ENS_STD2, ENS_KEPT, ENS_UMEAN, ENS_USTD };
+// Unwrapped precession phase atan2(Sz, Sy) + 2 pi turns of n particles into dst.
+int launch_gather_phase(const double* Sy, const double* Sz, const int32_t* turns, int64_t n, double* dst,
+                        void* stream);
 
 // Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
 // cast to int (0 = success).

@@ -69,6 +69,7 @@ __device__ __forceinline__ void write_snap(const RunArgs& a, int64_t i, int w, c
   reinterpret_cast<uint64_t*>(b + o[11])[i] = p.n_coll;
   reinterpret_cast<uint64_t*>(b + o[12])[i] = p.n_bounce;
   reinterpret_cast<uint64_t*>(b + o[13])[i] = p.n_steps;
+  reinterpret_cast<int32_t*>(b + o[14])[i] = p.turns;
 }
 
 // ------------------------------------------------------------------ set constants
@@ -122,6 +123,7 @@ __device__ __forceinline__ bool window_nested(PState& p, const SetParams& P, dou
           } while (res == 0);
         }
         tempH = g.h;
+        p.turns += g.turns;
         if (res > 0) res = 0;
       }
       if (P.keep) p.h = tempH;
@@ -192,6 +194,7 @@ __global__ void k_pack(RunArgs a, int slot) {
   reinterpret_cast<uint64_t*>(b + o[11])[i] = a.s.n_coll[i];
   reinterpret_cast<uint64_t*>(b + o[12])[i] = a.s.n_bounce[i];
   reinterpret_cast<uint64_t*>(b + o[13])[i] = a.s.n_steps[i];
+  reinterpret_cast<int32_t*>(b + o[14])[i] = a.s.turns[i];
 }
 
 // ------------------------------------------------------------------ persistent
@@ -285,6 +288,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent(RunArgs a) {
     }
     if (r != 0) {
       tempH = g.h;
+      p.turns += g.turns;
       if (P->keep) p.h = tempH;
       if (r < 0) {
         p.stop = true;
@@ -400,6 +404,7 @@ __device__ __forceinline__ DeviceState state_slot(const DeviceState& b, int64_t 
   ST_OFF(t) ST_OFF(px) ST_OFF(py) ST_OFF(pz) ST_OFF(vx) ST_OFF(vy) ST_OFF(vz) ST_OFF(Sx) ST_OFF(Sy) ST_OFF(Sz)
   ST_OFF(h) ST_OFF(next_gas) ST_OFF(rx) ST_OFF(ry) ST_OFF(rz) ST_OFF(rw) ST_OFF(rspare) ST_OFF(rhas) ST_OFF(fail)
   ST_OFF(n_coll) ST_OFF(n_bounce) ST_OFF(n_steps) ST_OFF(stop) ST_OFF(coll) ST_OFF(wall) ST_OFF(w_done)
+  ST_OFF(turns)
 #undef ST_OFF
   return s;
 }
@@ -633,6 +638,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
       }
       if (r != 0) {
         tempH = g.h;
+        tp.turns += g.turns;
         if (P->keep) tp.h = tempH;
         if (r < 0) {
           s_fail = r;

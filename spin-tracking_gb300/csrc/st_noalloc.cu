@@ -68,13 +68,13 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Caller buffer layout: the state arrays in this order, each n elements,
 // each starting on a 256-byte boundary.
-constexpr int kNumFields = 27;
+constexpr int kNumFields = 28;
 constexpr size_t kElem[kNumFields] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8,  // t pos_xyz v_xyz S_xyz
                                       4, 8, 8, 8,                    // fail n_coll n_bounce n_steps
                                       8, 8,                          // h next_gas
                                       8, 8, 8, 8, 8, 1,              // rng x y z w spare has
                                       1, 1, 1,                       // stop coll wall
-                                      4, 4};                         // set w_done
+                                      4, 4, 4};                      // set w_done turns
 
 size_t state_bytes(int64_t n) {
   const size_t m = (size_t)(n > 0 ? n : 1);
@@ -103,7 +103,7 @@ DeviceState carve(void* base, int64_t n) {
   s.rx = (uint64_t*)f[16]; s.ry = (uint64_t*)f[17]; s.rz = (uint64_t*)f[18]; s.rw = (uint64_t*)f[19];
   s.rspare = (double*)f[20]; s.rhas = (uint8_t*)f[21];
   s.stop = (uint8_t*)f[22]; s.coll = (uint8_t*)f[23]; s.wall = (uint8_t*)f[24];
-  s.set = (int32_t*)f[25]; s.w_done = (int32_t*)f[26];
+  s.set = (int32_t*)f[25]; s.w_done = (int32_t*)f[26]; s.turns = (int32_t*)f[27];
   return s;
 }
 

@@ -28,8 +28,8 @@ __all__ = [
 ]
 
 SNAP_FIELDS = ("t", "pos_x", "pos_y", "pos_z", "v_x", "v_y", "v_z", "S_x", "S_y", "S_z", "fail", "n_coll",
-               "n_bounce", "n_steps")
-_SNAP_DTYPES = (np.float64,) * 10 + (np.int32, np.uint64, np.uint64, np.uint64)
+               "n_bounce", "n_steps", "turns")
+_SNAP_DTYPES = (np.float64,) * 10 + (np.int32, np.uint64, np.uint64, np.uint64, np.int32)
 
 
 def default_options() -> Options:
@@ -132,7 +132,7 @@ class Particles:
         return int(load().st_snapshot_bytes(self._ctx))
 
     def snapshot_offsets(self) -> list[int]:
-        return [int(load().st_snapshot_field_offset(self._ctx, k)) for k in range(14)]
+        return [int(load().st_snapshot_field_offset(self._ctx, k)) for k in range(len(SNAP_FIELDS))]
 
     def device_state(self) -> DeviceSoA:
         d = DeviceSoA()
@@ -167,6 +167,11 @@ class Particles:
         windows_per_checkpoint: state checkpoints for replays when the tape
         does not fit (0: automatic)."""
         check(load().st_adjoint_record(self._ctx, int(w_end), int(tape_bytes), int(windows_per_checkpoint)))
+
+    def gather_phase(self, dst_ptr: int) -> None:
+        """Unwrapped precession phase atan2(Sz, Sy) + 2 pi turns of every particle into a
+        dense device array (one double per particle) at dst_ptr."""
+        check(load().st_gather_phase(self._ctx, ctypes.c_void_p(dst_ptr)))
 
     def ensemble(self, set_index: int = 0, snap_ptr: int = 0) -> dict:
         """Mean spin, polarisation, aligned/clipped precession phase and frequency

@@ -65,7 +65,8 @@ class Ensemble(ctypes.Structure):
     _fields_ = [("t", c_double), ("n_valid", c_int64), ("n_phase", c_int64), ("mean_S", c_double * 3),
                 ("polarisation", c_double), ("phase_mean", c_double), ("phase_std", c_double),
                 ("phase_stderr", c_double), ("phase_expected", c_double), ("freq_shift", c_double),
-                ("freq_shift_err", c_double)]
+                ("freq_shift_err", c_double), ("phase_unwrapped_mean", c_double),
+                ("phase_unwrapped_std", c_double), ("freq_shift_unwrapped", c_double)]
 
 
 class Counters(ctypes.Structure):
@@ -119,6 +120,7 @@ _SIGS = {
     "st_adjoint_record": (c_int, [c_void_p, c_int, c_size_t, c_int]),
     "st_adjoint_get_stats": (c_int, [c_void_p, POINTER(AdjointStats)]),
     "st_ensemble_stats": (c_int, [c_void_p, c_void_p, c_int, POINTER(Ensemble)]),
+    "st_gather_phase": (c_int, [c_void_p, c_void_p]),
     "st_adjoint_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
     "st_adjoint_backward_multi": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int]),
     "st_run_noalloc": (c_int, [POINTER(Options), c_int, c_void_p, POINTER(c_size_t), c_int, c_void_p]),
