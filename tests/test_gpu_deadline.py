@@ -1,0 +1,40 @@
+"""The device time budget (st_set_deadline): a run that runs out of it stops
+cleanly with ST_ERR_DEADLINE (lanes check %globaltimer, no kernel spins on
+anything), the context stays usable, and calling again resumes from the
+particles' last window-end checkpoints: the final state equals an
+uninterrupted run's bit for bit, for both kernels."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import spintrack as st
+from spintrack._capi import ST_ERR_DEADLINE
+
+pytestmark = pytest.mark.gpu
+
+
+def deadline_options():
+    return st.derive(st.make_options(numParticles=4096, dist="M", T=4.2, diffuse=0.1, gas_coll=False, gravity=True,
+                                     Gx=(0.0, 0.0, 1e-9), E=(0.0, 0.0, 75e5), yi=(0.0, 0.0, 1.0), tf=0.2,
+                                     ioutInt=0.05, seed=17))
+
+
+@pytest.mark.parametrize("kernel", [st.KERNEL_PERSISTENT, st.KERNEL_PLAIN], ids=["persistent", "plain"])
+def test_deadline_stops_and_the_next_call_resumes(gpu, kernel):
+    opt = deadline_options()
+    nw = st.num_windows(opt)
+    with st.Particles(opt) as p:
+        p.init_particles()
+        assert p.run_windows(0, nw, kernel) == 0
+        ref = p.output_data()
+        p.init_particles()
+        p.set_deadline(1e-4)  # far shorter than the run
+        assert p.run_windows(0, nw, kernel) == ST_ERR_DEADLINE
+        p.set_deadline(0.0)
+        for _ in range(3):  # the next call finishes what is left
+            if p.run_windows(0, nw, kernel) == 0:
+                break
+        got = p.output_data()
+    for f in ref:
+        np.testing.assert_array_equal(got[f], ref[f], err_msg=f)
