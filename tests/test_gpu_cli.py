@@ -11,9 +11,7 @@ from conftest import GOLDEN
 import spintrack as st
 from spintrack.build import CLI
 
-pytestmark = pytest.mark.gpu
-
-
+@pytest.mark.gpu
 @pytest.mark.parametrize("kernel", ["persistent", "plain"])
 def test_cli_writes_the_same_file_as_main_analysis(gpu, tmp_path, kernel):
     params = GOLDEN / "c1_precess.params"
@@ -26,6 +24,6 @@ def test_cli_writes_the_same_file_as_main_analysis(gpu, tmp_path, kernel):
     assert out_cli.read_bytes() == out_lib.read_bytes()
 
 
-def test_cli_usage_error_without_arguments(gpu):
+def test_cli_usage_error_without_arguments(stlib):
     r = subprocess.run([str(CLI)], capture_output=True, text=True, timeout=60)
     assert r.returncode != 0 and "Expects" in (r.stdout + r.stderr)
