@@ -17,6 +17,11 @@
 //                                     (src/integrator.cpp:90, :251) over one
 //                                     ballistic segment from (p, v) at t0;
 //                                     prints ret, y, h
+//   ref_probe magnus|rk45q|rkf45|rkf45q PARAMS ...same...
+//                                     integrateMagnusCFET (:625),
+//                                     integrateRK45Quaternion (:441),
+//                                     integrateRKF45 (:339),
+//                                     integrateRKF45Quaternion (:530) likewise
 //   ref_probe events PARAMS NSEG      per particle after init: NSEG rounds of
 //                                     calc_next_collision_time + update +
 //                                     sanity_check (src/particle.cpp:121-444)
@@ -113,8 +118,10 @@ int main(int argc, char** argv) {
     }
     return 0;
   }
-  if (!std::strcmp(cmd, "dop") || !std::strcmp(cmd, "rk45")) {
-    if (argc < 16) { std::fprintf(stderr, "dop/rk45 need 13 numbers\n"); return 2; }
+  const bool stepper = !std::strcmp(cmd, "dop") || !std::strcmp(cmd, "rk45") || !std::strcmp(cmd, "magnus") ||
+                       !std::strcmp(cmd, "rk45q") || !std::strcmp(cmd, "rkf45") || !std::strcmp(cmd, "rkf45q");
+  if (stepper) {
+    if (argc < 16) { std::fprintf(stderr, "%s needs 13 numbers\n", cmd); return 2; }
     double vals[13];
     for (int j = 0; j < 13; ++j) vals[j] = std::strtod(argv[3 + j], nullptr);
     double t0 = vals[0], tf = vals[1];
@@ -125,8 +132,13 @@ int main(int argc, char** argv) {
     (void)vals[12];
     // end-of-segment state is only used by the reference for signature parity
     coords p_new = p, v_new = v;
-    int ret = !std::strcmp(cmd, "dop") ? integrateDOP(t0, tf, y, p, p_new, v, v_new, opt, h)
-                                      : integrateRK45(t0, tf, y, p, p_new, v, v_new, opt, h);
+    int ret;
+    if (!std::strcmp(cmd, "dop")) ret = integrateDOP(t0, tf, y, p, p_new, v, v_new, opt, h);
+    else if (!std::strcmp(cmd, "rk45")) ret = integrateRK45(t0, tf, y, p, p_new, v, v_new, opt, h);
+    else if (!std::strcmp(cmd, "magnus")) ret = integrateMagnusCFET(t0, tf, y, p, p_new, v, v_new, opt, h);
+    else if (!std::strcmp(cmd, "rk45q")) ret = integrateRK45Quaternion(t0, tf, y, p, p_new, v, v_new, opt, h);
+    else if (!std::strcmp(cmd, "rkf45")) ret = integrateRKF45(t0, tf, y, p, p_new, v, v_new, opt, h);
+    else ret = integrateRKF45Quaternion(t0, tf, y, p, p_new, v, v_new, opt, h);
     std::printf("r %d", ret);
     hx(y.x); hx(y.y); hx(y.z); hx(h);
     std::printf("\n");

@@ -586,6 +586,208 @@ int or_integrate_rk45(const or_options *o, double t0, double tf, or_vec3 *yio, c
   }
 }
 
+/* ------------------------------------------------------------ integrator types 2-5
+ * Tableaux of include/coeff.h:220-320 (RKF45COEF, CFET8, CFET6, GL5) as
+ * shortest round-trip doubles (identical bits). */
+static const double rkf_A[7] = {0.0, 0.0, 0.25, 0.375, 0.9230769230769231, 1.0, 0.5};
+static const double rkf_B21 = 0.25;
+static const double rkf_B3[2] = {0.09375, 0.28125};
+static const double rkf_B4[3] = {0.8793809740555303, -3.277196176604461, 3.3208921256258535};
+static const double rkf_B5[4] = {2.0324074074074074, -8.0, 7.173489278752436, -0.20589668615984405};
+static const double rkf_B6[5] = {-0.2962962962962963, 2.0, -1.3816764132553607, 0.4529727095516569, -0.275};
+static const double rkf_C[6] = {0.11851851851851852, 0.0, 0.5189863547758284, 0.5061314903420167, -0.18,
+                                0.03636363636363636};
+static const double rkf_CR[6] = {0.11574074074074074, 0.0, 0.5489278752436647, 0.5353313840155945, -0.2, 0.0};
+static const double rk_C5[5] = {0.1111111111111111, 0.0, 0.45, 0.35555555555555557, 0.08333333333333333};
+/* CFET8 G[i][j] = G(i+1)(j+1), CFET6 H likewise, Gauss-Legendre nodes X */
+static const double cfet8_G[6][5] = {
+    {-0.005984812750244602, 0.020217897716672675, -0.03646660716686794, 0.04245408899634467, 0.14949496424802844},
+    {0.02512881778391826, -0.08955337580937157, 0.19032828600393248, 0.28920194841768715, -0.03568486888016069},
+    {-0.04972613261435144, 0.6572496090804754, 0.11725149008224456, -0.43611911073577403, 0.18080345083145516},
+    {0.0464837870954061, -0.6265183532355708, -0.11144873822286155, 0.4154988625423615, -0.17224148557040517},
+    {0.015567390500242426, -0.0677120111619075, -0.15241336773272682, -0.08803798509100481, -0.0013284996209207986},
+    {-0.034049168494873015, 0.12263276452977083, 0.2699423185170027, 0.12263276452977094, -0.03404916849487304}};
+static const double cfet6_H[3][5] = {
+    {-0.007431519425246311, 0.022452824849980513, -0.03620393417193995, 0.0409779901800809, 0.1516046385671249},
+    {0.03095749686312404, -0.10116885619385878, 0.1997455955716367, 0.3010242365525433, -0.055594729593982636},
+    {-0.001072443882925378, -0.023971860139062367, -0.04263887835494916, -0.023971860139062388,
+     -0.0010724438829253797}};
+static const double gl5_X[5] = {0.046910077030668074, 0.2307653449471585, 0.5, 0.7692346550528415,
+                                0.9530899229693319};
+
+/* findCrossTerm (src/integrator.cpp:63-70): gamma * B at time t. */
+static or_vec3 omega(const or_options *o, double t, double t0, const or_vec3 *p_old, const or_vec3 *v_old) {
+  or_vec3 p, v;
+  or_interpolate(o, t, t0, p_old, v_old, &p, &v);
+  or_vec3 G = v3(vdot(p, o->Gx), vdot(p, o->Gy), vdot(p, o->Gz));
+  or_vec3 pulse = v3(0.0, 0.0, o->a * cos(o->w * t));
+  or_vec3 B = vadd(vadd(vadd(pulse, o->B0), vscale(1.0 / OR_C2, vcross(v, o->E))), G);
+  return vscale(o->gamma, B);
+}
+
+/* Quaternions (w, x, y, z) of src/quaternion.cpp: qMult, qv_mult (v as the
+ * pure quaternion (0, v), rotated as q v q*), rodriguezQuat and rodriguez. */
+typedef struct { double w, x, y, z; } or_quat;
+static or_quat qmul(or_quat a, or_quat b) {
+  or_quat r;
+  r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+  r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+  r.y = a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z;
+  r.z = a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x;
+  return r;
+}
+static or_vec3 qrotate(or_quat q, or_vec3 v) {
+  or_quat p = {0.0, v.x, v.y, v.z}, qc = {q.w, -q.x, -q.y, -q.z};
+  p = qmul(qmul(q, p), qc);
+  return v3(p.x, p.y, p.z);
+}
+/* rotation by |k| dt about -k/|k|, as a unit quaternion */
+static or_quat rot_quat(or_vec3 k, double dt) {
+  double angle = vlen(k);
+  or_vec3 n = vdivs(k, angle);
+  double h = angle * dt;
+  n = vscale(-sin(h / 2.0), n);
+  or_quat r = {cos(h / 2.0), n.x, n.y, n.z};
+  return r;
+}
+/* v rotated by the angle |k| about -k/|k| (Rodrigues' formula) */
+static or_vec3 rodrigues(or_vec3 k, or_vec3 v) {
+  const double angle = vlen(k);
+  const double s = sin(angle);
+  const double c = cos(angle);
+  return vadd(vadd(vscale(c, v), vscale(s / angle, vcross(v, k))), vscale(vdot(k, v) * (1.0 - c) / (angle * angle), k));
+}
+
+/* (c[0] B[0] + ... + c[4] B[4]) h with the coefficients taken forwards, or
+ * backwards (c[4] B[0] + ... + c[0] B[4]) when rev is set. */
+static or_vec3 magnus_exponent(const double c[5], int rev, const or_vec3 B[5], double h) {
+  or_vec3 s = vscale(c[rev ? 4 : 0], B[0]);
+  for (int j = 1; j < 5; ++j) s = vadd(s, vscale(c[rev ? 4 - j : j], B[j]));
+  return vscale(h, s);
+}
+
+/* One attempt's proposal (ws) and error vector (te) of types 2-5 at (t, y, h).
+ * yy carries RKF45's stage state between attempts (its k1 quirk). */
+static void ext_stages(const or_options *o, int type, double t, double h, or_vec3 y, or_vec3 *yy, double t0,
+                       const or_vec3 *p_old, const or_vec3 *v_old, or_vec3 *ws, or_vec3 *te) {
+  if (type == 2) {
+    /* integrateMagnusCFET (src/integrator.cpp:670-698): the CFET8 product
+     * applied from its 11th exponent inwards, and the CFET6 one beside it */
+    or_vec3 B[5];
+    for (int i = 0; i < 5; ++i) B[i] = omega(o, t + gl5_X[i] * h, t0, p_old, v_old);
+    or_vec3 y8 = y;
+    for (int r = 0; r < 5; ++r) y8 = rodrigues(magnus_exponent(cfet8_G[r], 1, B, h), y8);   /* k11 .. k7 */
+    for (int r = 5; r >= 0; --r) y8 = rodrigues(magnus_exponent(cfet8_G[r], 0, B, h), y8);  /* k6 .. k1 */
+    or_vec3 y6 = y;
+    for (int r = 0; r < 2; ++r) y6 = rodrigues(magnus_exponent(cfet6_H[r], 1, B, h), y6);   /* k5, k4 */
+    for (int r = 2; r >= 0; --r) y6 = rodrigues(magnus_exponent(cfet6_H[r], 0, B, h), y6);  /* k3 .. k1 */
+    *ws = y8;
+    *te = vsub(y8, y6);
+  } else if (type == 3 || type == 5) {
+    /* integrateRK45Quaternion (:476-497) / integrateRKF45Quaternion (:565-586):
+     * the stage fields at the tableau's nodes, composed as rotations */
+    const double *A = (type == 3) ? rk_A : rkf_A;
+    const double *W = (type == 3) ? rk_CH : rkf_C;
+    const double *E = (type == 3) ? rk_C5 : rkf_C;
+    or_vec3 k[7];
+    k[1] = omega(o, t, t0, p_old, v_old);
+    for (int s = 2; s <= 6; ++s) k[s] = omega(o, t + A[s] * h, t0, p_old, v_old);
+    or_quat qw = rot_quat(k[1], h * W[0]), qe = rot_quat(k[1], h * E[0]);
+    for (int s = 2; s <= 6; ++s) qw = qmul(rot_quat(k[s], h * W[s - 1]), qw);
+    for (int s = 2; s <= 5; ++s) qe = qmul(rot_quat(k[s], h * E[s - 1]), qe);
+    *ws = qrotate(qw, y);
+    *te = vsub(*ws, qrotate(qe, y));
+  } else {
+    /* integrateRKF45 (:384-396), with RK45's first-stage quirk */
+    or_vec3 k[7];
+    k[1] = bloch(o, t, *yy, t0, p_old, v_old);
+    *yy = vadd(y, vscale(h * rkf_B21, k[1]));
+    k[2] = bloch(o, t + rkf_A[2] * h, *yy, t0, p_old, v_old);
+    *yy = vadd(vadd(y, vscale(h * rkf_B3[0], k[1])), vscale(h * rkf_B3[1], k[2]));
+    k[3] = bloch(o, t + rkf_A[3] * h, *yy, t0, p_old, v_old);
+    *yy = y;
+    for (int j = 0; j < 3; ++j) *yy = vadd(*yy, vscale(h * rkf_B4[j], k[1 + j]));
+    k[4] = bloch(o, t + rkf_A[4] * h, *yy, t0, p_old, v_old);
+    *yy = y;
+    for (int j = 0; j < 4; ++j) *yy = vadd(*yy, vscale(h * rkf_B5[j], k[1 + j]));
+    k[5] = bloch(o, t + rkf_A[5] * h, *yy, t0, p_old, v_old);
+    *yy = y;
+    for (int j = 0; j < 5; ++j) *yy = vadd(*yy, vscale(h * rkf_B6[j], k[1 + j]));
+    k[6] = bloch(o, t + rkf_A[6] * h, *yy, t0, p_old, v_old);
+    or_vec3 wsum = vscale(rkf_C[0], k[1]), tsum = vscale(rkf_CR[0], k[1]);
+    for (int j = 1; j < 6; ++j) wsum = vadd(wsum, vscale(rkf_C[j], k[1 + j]));
+    for (int j = 1; j < 6; ++j) tsum = vadd(tsum, vscale(rkf_CR[j], k[1 + j]));
+    *ws = vadd(y, vscale(h, wsum));
+    *te = vscale(h, tsum);  /* the whole fourth-order increment, as the reference has it */
+  }
+}
+
+/* integrateMagnusCFET (src/integrator.cpp:625-722), integrateRK45Quaternion
+ * (:441-528), integrateRKF45 (:339-439) and integrateRKF45Quaternion
+ * (:530-623), selected by o->integratorType 2, 3, 4, 5.  Their shared step
+ * controller differs from RK45's: the segment end is tested before the
+ * hmax/hmin limits, and a fixed step never looks at the segment end (such a
+ * run ends after nmax attempts, -2).  Returns 0, -1 (h < hmin) or -2. */
+int or_integrate_ext(const or_options *o, double t0, double tf, or_vec3 *yio, const or_vec3 *p_old,
+                     const or_vec3 *v_old, double *hio) {
+  const int type = o->integratorType;
+  or_vec3 y = *yio, yy = v3(0.0, 0.0, 0.0);
+  double h = *hio, t = t0, lastH = h, prev_ratio = 1.0;
+  int stop = 0;
+  unsigned int nstep = 0;
+  const double e1 = 0.7 / 7.0, e2 = -0.4 / 7.0;
+  for (;;) {
+    nstep++;
+    if (nstep > o->nmax) {
+      *yio = y;
+      *hio = h;
+      return -2;
+    }
+    if (g_counters) {
+#pragma omp atomic
+      g_counters->ext_attempts++;
+    }
+    double endDt = tf - t;
+    lastH = h;
+    if (o->fixedStepSize) {
+      h = o->h;
+    } else if (h >= endDt) {
+      h = endDt;
+      stop = 1;
+    } else {
+      lastH = h;
+      stop = 0;
+      if (h > o->hmax) {
+        h = std_min(h, o->hmax);
+      } else if (h < o->hmin) {
+        *yio = y;
+        *hio = h;
+        return -1;
+      }
+    }
+    or_vec3 ws, te;
+    ext_stages(o, type, t, h, y, &yy, t0, p_old, v_old, &ws, &te);
+    double error = std_max(vlen(te), 1.0e-16);
+    double tol = o->rtol;
+    double ratio = tol / error;
+    double q = pow(ratio, e1) * pow(prev_ratio, e2);
+    q = std_min(q, 4.0);
+    if ((q > 0.81 && error < 2 * tol) || o->fixedStepSize) {
+      y = ws;
+      t += h;
+      if (stop) {
+        *yio = y;
+        *hio = lastH;
+        return 0;
+      }
+    } else {
+      if (stop) stop = 0;
+    }
+    if (!o->fixedStepSize) h = h * q;
+    prev_ratio = ratio;
+  }
+}
+
 /* ------------------------------------------------------------ trajectory */
 /* calc_next_collision_time (src/particle.cpp:121-257) */
 static void next_collision(const or_options *o, double t, double tf, or_vec3 v, or_vec3 pos, double *next_gas,
@@ -832,6 +1034,8 @@ static void run_particle(const or_options *o, or_particles *p, int i, double nex
         res = or_integrate_dop(o, p->t_old[i], p->t[i], &p->S[i], &p->pos_old[i], &p->v_old[i], &hcarry);
       else if (o->integratorType == 1)
         res = or_integrate_rk45(o, p->t_old[i], p->t[i], &p->S[i], &p->pos_old[i], &p->v_old[i], &hcarry);
+      else if (o->integratorType >= 2 && o->integratorType <= 5)
+        res = or_integrate_ext(o, p->t_old[i], p->t[i], &p->S[i], &p->pos_old[i], &p->v_old[i], &hcarry);
       if (o->keepStepSize) p->h[i] = hcarry;
       if (res < 0) {
         p->stop[i] = true;

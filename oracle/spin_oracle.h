@@ -81,6 +81,10 @@ int or_integrate_dop(const or_options *opt, double t0, double tf, or_vec3 *y, co
                      const or_vec3 *v_old, double *h);
 int or_integrate_rk45(const or_options *opt, double t0, double tf, or_vec3 *y, const or_vec3 *p_old,
                       const or_vec3 *v_old, double *h);
+/* integratorType 2-5 (src/integrator.cpp:339-722): Magnus CFET8, RK45 with
+ * quaternions, RKF45, RKF45 with quaternions; the type is opt->integratorType. */
+int or_integrate_ext(const or_options *opt, double t0, double tf, or_vec3 *y, const or_vec3 *p_old,
+                     const or_vec3 *v_old, double *h);
 
 /* Ballistic interpolation (src/integrator.cpp:48-61). */
 void or_interpolate(const or_options *opt, double t, double t0, const or_vec3 *p_old, const or_vec3 *v_old,
@@ -102,7 +106,7 @@ double or_run_sample(const or_options *opt, int first, int count, int nthreads, 
 
 /* Instrumented count of DOP853 step attempts and segments, for the roofline
  * work model: filled by or_run_until when non-null. */
-typedef struct { uint64_t dop_attempts, rk45_attempts, segments; } or_counters;
+typedef struct { uint64_t dop_attempts, rk45_attempts, segments, ext_attempts; } or_counters;
 void or_set_counters(or_counters *c);
 
 /* Frozen accepted-step log for finite-difference checks: mode 1 records every

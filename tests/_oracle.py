@@ -35,7 +35,8 @@ class Particles(ctypes.Structure):
 
 
 class Counters(ctypes.Structure):
-    _fields_ = [("dop_attempts", c_uint64), ("rk45_attempts", c_uint64), ("segments", c_uint64)]
+    _fields_ = [("dop_attempts", c_uint64), ("rk45_attempts", c_uint64), ("segments", c_uint64),
+                ("ext_attempts", c_uint64)]
 
 
 def build() -> None:
@@ -66,6 +67,7 @@ class Oracle:
             "or_run_until": (None, [P(Options), P(Particles), c_double, c_int]),
             "or_integrate_dop": (c_int, [P(Options), c_double, c_double, P(Vec3), P(Vec3), P(Vec3), P(c_double)]),
             "or_integrate_rk45": (c_int, [P(Options), c_double, c_double, P(Vec3), P(Vec3), P(Vec3), P(c_double)]),
+            "or_integrate_ext": (c_int, [P(Options), c_double, c_double, P(Vec3), P(Vec3), P(Vec3), P(c_double)]),
             "or_interpolate": (None, [P(Options), c_double, c_double, P(Vec3), P(Vec3), P(Vec3), P(Vec3)]),
             "or_event": (c_int, [P(Options), P(Particles), c_int, c_double]),
             "or_main_analysis": (c_int, [P(Options), ctypes.c_char_p, c_int, P(c_double)]),

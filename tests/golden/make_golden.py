@@ -53,6 +53,24 @@ CASES = {
     # RK45 with its first-stage quirk
     "rk45": dict(numParticles="4", dist="C", V="5", gas_coll="false", diffuse="0", gravity="true",
                  yi="0, 0, 1", integratorType="1", tf="0.004", ioutInt="0.001", **G_FULL),
+    # integratorType 2-5 (src/integrator.cpp:339-722)
+    "magnus": dict(numParticles="6", dist="M", T="4.2", gas_coll="false", diffuse="0.2", gravity="true",
+                   yi="0, 0, 1", integratorType="2", a="5e-6", w="6283.185307179586", hmax="1e-4", tf="0.02",
+                   ioutInt="0.005", seed="12", **G_FULL),
+    "rk45q": dict(numParticles="6", dist="M", T="4.2", gas_coll="false", diffuse="0.2", gravity="true",
+                  yi="0, 0, 1", integratorType="3", rtol="1e-10", tf="0.02", ioutInt="0.005", seed="13", **G_FULL),
+    "rkf45": dict(numParticles="6", dist="C", V="5", gas_coll="false", diffuse="0.2", gravity="true",
+                  yi="0, 1, 0", integratorType="4", rtol="1e-3", tf="0.02", ioutInt="0.005", seed="14", **G_FULL),
+    "rkf45q": dict(numParticles="6", dist="C", V="5", T="0.4", gas_coll="true", diffuse="0.2", gravity="true",
+                   yi="0, 0, 1", integratorType="5", rtol="1e-6", tf="0.02", ioutInt="0.005", seed="15", **G_FULL),
+    # RKF45's error estimate is its whole fourth-order increment: at rtol 1e-12
+    # the step shrinks below hmin at once (-1)
+    "rkf45_hmin": dict(numParticles="4", dist="C", V="5", gas_coll="false", diffuse="0", gravity="true",
+                       yi="0, 0, 1", integratorType="4", tf="0.01", ioutInt="0.005", **G_FULL),
+    # a fixed step of types 2-5 never tests the segment end: nmax attempts, then -2
+    "magnus_fixed": dict(numParticles="4", dist="C", V="5", gas_coll="false", diffuse="0", gravity="true",
+                         yi="0, 0, 1", integratorType="2", fixedStepSize="true", h="1e-4", nmax="40", tf="0.01",
+                         ioutInt="0.005", **G_FULL),
     "nograv": dict(numParticles="16", dist="C", V="5", gas_coll="false", diffuse="0", gravity="false",
                    yi="0, 0, 1", tf="0.3", ioutInt="0.05", **G_FULL),
     "keep": dict(numParticles="8", dist="M", T="4.2", gas_coll="false", diffuse="0", gravity="true", yi="0, 0, 1",
@@ -141,6 +159,30 @@ def main() -> int:
         lines_rk.append(f"{pf_.name} {' '.join(args)} | " + run([str(probe), "rk45", str(pf_), *args]).stdout.strip())
     (HERE / "probe_dop.txt").write_text("\n".join(lines_dop) + "\n")
     (HERE / "probe_rk45.txt").write_text("\n".join(lines_rk) + "\n")
+    # integratorType 2-5 over single segments: free precession, a moving
+    # particle in the full field, and the same with the dressing pulse
+    pd = HERE / "probe_pulse.params"
+    pd.write_text(params_text(dict(numParticles="6", dist="C", V="5", gas_coll="false", gravity="true",
+                                   yi="0, 0, 1", a="5e-6", w="6283.185307179586", hmax="1e-4", tf="0.2",
+                                   ioutInt="0.05", seed="17", **G_FULL)))
+    ext_segs = [
+        (pf, ["0.1", "0.1005", "0", "0", "1", "0", "0", "0", "0", "0", "0", "1e-5", "0"]),
+        (pp, ["0.0", "0.0004", "0", "0", "1", "0.01", "-0.02", "0.05", "3", "-2", "1", "1e-5", "0"]),
+        (pd, ["0.25", "0.2504", "0.6", "0.0", "0.8", "-0.03", "0.04", "-0.15", "-1.5", "4", "0.5", "2e-5", "0"]),
+    ]
+    for cmd in ("magnus", "rk45q", "rkf45", "rkf45q"):
+        lines = []
+        for pf_, args in ext_segs:
+            # RKF45 (and its quaternion form at rtol 1e-12) fails with -1; with a
+            # loose tolerance (params differing only in rtol) it takes steps
+            variants = [pf_]
+            if cmd in ("rkf45", "rkf45q"):
+                pz = HERE / f"{pf_.stem}_rtol3.params"
+                pz.write_text(pf_.read_text().replace("rtol, 1e-12", "rtol, 1e-3"))
+                variants.append(pz)
+            for pz in variants:
+                lines.append(f"{pz.name} {' '.join(args)} | " + run([str(probe), cmd, str(pz), *args]).stdout.strip())
+        (HERE / f"probe_{cmd}.txt").write_text("\n".join(lines) + "\n")
     print("probes written")
     return 0
 

@@ -109,14 +109,21 @@ def test_events_match_reference(oracle):
         oracle.free(p)
 
 
-@pytest.mark.parametrize("which", ["dop", "rk45"])
+EXT_TYPE = {"magnus": 2, "rk45q": 3, "rkf45": 4, "rkf45q": 5}
+
+
+@pytest.mark.parametrize("which", ["dop", "rk45", "magnus", "rk45q", "rkf45", "rkf45q"])
 def test_segment_steppers_match_reference(oracle, which):
-    """integrateDOP / integrateRK45 over single ballistic segments."""
-    fn = oracle.L.or_integrate_dop if which == "dop" else oracle.L.or_integrate_rk45
+    """integrateDOP / integrateRK45 / integrateMagnusCFET /
+    integrateRK45Quaternion / integrateRKF45 / integrateRKF45Quaternion over
+    single ballistic segments, accepted steps and hmin failures alike."""
+    fn = {"dop": oracle.L.or_integrate_dop, "rk45": oracle.L.or_integrate_rk45}.get(which, oracle.L.or_integrate_ext)
     for line in (GOLDEN / f"probe_{which}.txt").read_text().splitlines():
         lhs, rhs = line.split("|")
         a = lhs.split()
         opt = oracle.parse_file(GOLDEN / a[0])
+        if which in EXT_TYPE:
+            opt.integratorType = EXT_TYPE[which]
         v = [float(x) for x in a[1:]]
         y = Vec3(*v[2:5])
         p0 = Vec3(*v[5:8])
