@@ -27,7 +27,7 @@ extern "C" {
 #define ST_OK 0
 #define ST_ERR_ARG (-1)         /* bad argument or option value */
 #define ST_ERR_CUDA (-2)        /* CUDA runtime error (message in st_last_error) */
-#define ST_ERR_UNSUPPORTED (-3) /* option outside the implemented path (e.g. integratorType 2-6) */
+#define ST_ERR_UNSUPPORTED (-3) /* option outside the implemented path (e.g. integratorType 6) */
 #define ST_ERR_IO (-4)          /* file could not be opened or written */
 #define ST_ERR_STATE (-5)       /* call out of order (e.g. run before init) */
 #define ST_ERR_DEADLINE (-6)    /* device time budget ran out; state is saved and resumable */
@@ -163,8 +163,8 @@ const char *st_launch_variant_name(int variant);
  * When it runs out, kernels save the particle state and the call returns
  * ST_ERR_DEADLINE; calling again resumes. */
 int st_set_deadline(st_ctx *ctx, double seconds);
-/* Work counters of the last run call: DOP853 and RK45 step attempts,
- * trajectory segments, and kernels launched.  st_run_windows enqueues its
+/* Work counters of the last run call: DOP853, RK45 and integratorType 2-5
+ * step attempts, trajectory segments, and kernels launched.  st_run_windows enqueues its
  * launches as one CUDA graph, captured on the first call with a given
  * (kernel, window range, snapshot buffer, launch configuration, deadline) and
  * replayed by later calls: graph_launches = 1 for such a call, graph_captures
@@ -172,6 +172,7 @@ int st_set_deadline(st_ctx *ctx, double seconds);
 typedef struct st_counters {
   uint64_t dop_attempts, rk45_attempts, segments, kernel_launches;
   uint64_t graph_launches, graph_captures;
+  uint64_t ext_attempts;  /* step attempts of integratorType 2-5 */
 } st_counters;
 int st_get_counters(const st_ctx *ctx, st_counters *out);
 

@@ -95,9 +95,8 @@ bool to_bool(const std::string& s) {
 // ---------------------------------------------------------------- params
 int build_params(const st_options& o, int64_t first, SetParams* P) {
   if (o.numParticles < 0) return fail(ST_ERR_ARG, "numParticles must be >= 0");
-  if (o.integratorType >= 2 && o.integratorType <= 6)
-    return fail(ST_ERR_UNSUPPORTED, "integratorType " + std::to_string(o.integratorType) +
-                                        " (RKF45 / quaternion / Magnus / spectrum) is not implemented; use 0 (DOP853) or 1 (RK45)");
+  if (o.integratorType == 6)
+    return fail(ST_ERR_UNSUPPORTED, "integratorType 6 (spectrum) is not implemented; use 0-5");
   if (o.dist != 'C' && o.dist != 'M')
     return fail(ST_ERR_UNSUPPORTED, std::string("dist must be 'C' or 'M', got '") + o.dist + "'");
   if (!(o.ioutInt > 0.0)) return fail(ST_ERR_ARG, "ioutInt must be > 0");
@@ -269,23 +268,43 @@ int ctx_alloc(st_ctx* c) {
   return ST_OK;
 }
 
-// Work order for the persistent queue: sets grouped by integrator (RK45,
-// then DOP853, then trajectory-only), so that a warp's lanes run one step code
-// and do not diverge between two; within a group, longest expected particles
-// first, so the tail of the run is short.  Cost = simulated time, RK45
-// weighted 2000x (at rtol 1e-12 it takes ~4400x the attempts of DOP853, each
-// ~0.4x the work).
+// Work order for the persistent queue: sets grouped by integrator (the
+// fourth/fifth-order ones first: RK45, RK45 and RKF45 with quaternions,
+// RKF45; then Magnus, DOP853, trajectory-only), so that a warp's lanes run one
+// step code and do not diverge between two; within a group, longest expected
+// particles first, so the tail of the run is short.  Cost = simulated time,
+// the fourth/fifth-order types weighted 2000x (at rtol 1e-12 RK45 takes ~4400x
+// the attempts of DOP853, each ~0.4x the work).
+// Some set integrates with type 2-5: the runs take the EXT kernels.
+bool ctx_any_ext(const st_ctx* c) {
+  for (const auto& P : c->sets_h)
+    if (P.integrator >= 2 && P.integrator <= 5) return true;
+  return false;
+}
+
+int order_group(int it) {
+  switch (it) {
+    case 1: return 0;
+    case 3: return 1;
+    case 5: return 2;
+    case 4: return 3;
+    case 2: return 4;
+    case 0: return 5;
+    default: return 6;
+  }
+}
+double order_weight(int it) { return (it == 1 || it == 3 || it == 4 || it == 5) ? 2000.0 : 1.0; }
+
 int ctx_build_order(st_ctx* c) {
   if (c->order_d || c->sets_h.size() <= 1) return ST_OK;
   std::vector<int> idx(c->sets_h.size());
   for (size_t k = 0; k < idx.size(); ++k) idx[k] = (int)k;
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
     const SetParams &A = c->sets_h[a], &B = c->sets_h[b];
-    const int ga = A.integrator == 1 ? 0 : (A.integrator == 0 ? 1 : 2);
-    const int gb = B.integrator == 1 ? 0 : (B.integrator == 0 ? 1 : 2);
+    const int ga = order_group(A.integrator), gb = order_group(B.integrator);
     if (ga != gb) return ga < gb;
-    const double ca = (A.integrator == 1 ? 2000.0 : 1.0) * A.nwin * A.ioutInt;
-    const double cb = (B.integrator == 1 ? 2000.0 : 1.0) * B.nwin * B.ioutInt;
+    const double ca = order_weight(A.integrator) * A.nwin * A.ioutInt;
+    const double cb = order_weight(B.integrator) * B.nwin * B.ioutInt;
     return ca > cb;
   });
   std::vector<int64_t> order;
@@ -313,6 +332,7 @@ st::RunArgs make_args(st_ctx* c, int w_begin, int w_end, void* snap) {
   a.deadline_armed = 0;
   a.count_work = 1;
   a.any_gas = 0;
+  a.any_ext = ctx_any_ext(c) ? 1 : 0;
   for (const auto& P : c->sets_h) a.any_gas |= P.gas ? 1 : 0;
   return a;
 }
@@ -332,6 +352,7 @@ int end_run(st_ctx* c, int launches) {
   if (e != cudaSuccess) return fail(ST_ERR_CUDA, std::string("kernel execution: ") + cudaGetErrorString(e));
   c->last.dop_attempts = c->status_h->dop_attempts;
   c->last.rk45_attempts = c->status_h->rk45_attempts;
+  c->last.ext_attempts = c->status_h->ext_attempts;
   c->last.segments = c->status_h->segments;
   c->last.kernel_launches = (uint64_t)launches;
   c->last.graph_launches = 0;
@@ -829,7 +850,7 @@ int st_set_launch_config(st_ctx* c, const st_launch_config* cfg) {
   if (cfg->variant >= st::persistent_variant_count()) return fail(ST_ERR_ARG, "no such kernel variant");
   c->lc = *cfg;
   if (c->lc.variant >= 0 && c->lc.blocks_per_sm <= 0) {
-    c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, 0));
+    c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, ctx_any_ext(c) ? 1 : 0));
   }
   return ST_OK;
 }
@@ -1478,7 +1499,7 @@ namespace {
 // Tuned configurations, keyed by the workload's shape, reused by every later
 // context of the process.
 struct TuneKey {
-  int ntypes_mask;  // bit 0: a DOP853 set, bit 1: an RK45 set, bit 2: trajectory-only
+  int ntypes_mask;  // bit 0: a DOP853 set, bit 1: an RK45 set, bit 2: trajectory-only, bit 3 + t - 2: type t in 2-5
   int log2n;
   bool operator<(const TuneKey& o) const {
     return ntypes_mask != o.ntypes_mask ? ntypes_mask < o.ntypes_mask : log2n < o.log2n;
@@ -1491,7 +1512,11 @@ std::map<TuneKey, st_launch_config>& tune_cache() {
 
 int autotune(st_ctx* c) {
   TuneKey key{0, 0};
-  for (const auto& P : c->sets_h) key.ntypes_mask |= P.integrator == 0 ? 1 : (P.integrator == 1 ? 2 : 4);
+  for (const auto& P : c->sets_h) {
+    const int it = P.integrator;
+    key.ntypes_mask |= it == 0 ? 1 : it == 1 ? 2 : (it >= 2 && it <= 5) ? (8 << (it - 2)) : 4;
+  }
+  const int ext = ctx_any_ext(c) ? 1 : 0;
   while ((int64_t(1) << key.log2n) < c->n) ++key.log2n;
   auto it = tune_cache().find(key);
   if (it != tune_cache().end()) {
@@ -1504,17 +1529,19 @@ int autotune(st_ctx* c) {
   // decide and favour low occupancy), one short window on a scratch context,
   // so each candidate runs for tens of milliseconds: the window is capped at
   // 50 ms of simulated time for DOP853 sets (~250 attempts per particle at
-  // rtol 1e-12) and at 50 us for RK45 sets, whose step at rtol 1e-12 is
-  // thousands of times shorter.
+  // rtol 1e-12) and at 50 us for the fourth/fifth-order types (RK45, RKF45
+  // and their quaternion forms), whose step at rtol 1e-12 is thousands of
+  // times shorter.
   std::vector<st_options> sample = c->opts;
   int widest = 1;
   for (int v = 0; v < nv; ++v)
-    widest = std::max(widest, st::persistent_max_blocks_per_sm(v, 0) * st::persistent_variant_block(v));
+    widest = std::max(widest, st::persistent_max_blocks_per_sm(v, ext) * st::persistent_variant_block(v));
   const int64_t want = std::max<int64_t>((int64_t)c->sm_count * widest * 4, 1);
   const double frac = std::min(1.0, (double)want / (double)std::max<int64_t>(c->n, 1));
   for (auto& o : sample) {
     o.numParticles = o.numParticles > 0 ? std::max(1, (int)std::ceil(o.numParticles * frac)) : 0;
-    o.ioutInt = std::min(o.ioutInt, o.integratorType == 1 ? 5e-5 : 0.05);
+    const int it = o.integratorType;
+    o.ioutInt = std::min(o.ioutInt, (it == 1 || it == 3 || it == 4 || it == 5) ? 5e-5 : 0.05);
     o.tf = o.t0 + o.ioutInt;
   }
   st_ctx* s = nullptr;
@@ -1524,7 +1551,7 @@ int autotune(st_ctx* c) {
   // Each variant at its highest occupancy (its register budget is part of
   // the variant): on every workload measured, fewer resident blocks lost.
   for (int v = 0; v < nv; ++v) {
-    const int maxb = std::max(1, st::persistent_max_blocks_per_sm(v, 0));
+    const int maxb = std::max(1, st::persistent_max_blocks_per_sm(v, ext));
     {
       st_launch_config cfg{0, maxb, v};
       st_set_launch_config(s, &cfg);

@@ -1,5 +1,6 @@
 // Device building blocks of the hot path: the RNG, the ballistic trajectory
-// events, the field polynomial and single step attempts of DOP853 and RK45.
+// events, the field polynomial and single step attempts of DOP853, RK45 and
+// the integrator types 2-5 (Magnus CFET8, RK45 / RKF45 with quaternions, RKF45).
 //
 // Two arithmetic regimes:
 //  * Trajectory and RNG code reproduces the reference's doubles bit for bit
@@ -949,6 +950,272 @@ __device__ __forceinline__ int rk45_attempt(Seg& g, const SetParams& P, double& 
     const double ny = fma(h, wy, Sy), nz = fma(h, wz, Sz);
     g.turns += count_turn(Sy, Sz, ny, nz);
     Sx = fma(h, wx, Sx); Sy = ny; Sz = nz;
+    g.x += h;
+    if (stop) {
+      g.h = g.lastH;
+      return 1;
+    }
+  }
+  g.h = P.fixed ? h : h * q;
+  g.lnprev = lnr;
+  return 0;
+}
+
+// ------------------------------------------------------------ integrator types 2-5
+// Magnus CFET8 (src/integrator.cpp:625-722), RK45 with quaternions (:441-528),
+// RKF45 (:339-439) and RKF45 with quaternions (:530-623).
+namespace cfetc {
+__device__ __forceinline__ constexpr double x(int i) {
+  return i == 0 ? cfet::X1 : i == 1 ? cfet::X2 : i == 2 ? cfet::X3 : i == 3 ? cfet::X4 : cfet::X5;
+}
+// CFET8 row r (0-5), node j (0-4)
+__device__ __forceinline__ constexpr double g(int r, int j) {
+  switch (r * 8 + j) {
+    case 0: return cfet::G11;  case 1: return cfet::G12;  case 2: return cfet::G13;
+    case 3: return cfet::G14;  case 4: return cfet::G15;
+    case 8: return cfet::G21;  case 9: return cfet::G22;  case 10: return cfet::G23;
+    case 11: return cfet::G24; case 12: return cfet::G25;
+    case 16: return cfet::G31; case 17: return cfet::G32; case 18: return cfet::G33;
+    case 19: return cfet::G34; case 20: return cfet::G35;
+    case 24: return cfet::G41; case 25: return cfet::G42; case 26: return cfet::G43;
+    case 27: return cfet::G44; case 28: return cfet::G45;
+    case 32: return cfet::G51; case 33: return cfet::G52; case 34: return cfet::G53;
+    case 35: return cfet::G54; case 36: return cfet::G55;
+    case 40: return cfet::G61; case 41: return cfet::G62; case 42: return cfet::G63;
+    case 43: return cfet::G64; default: return cfet::G65;
+  }
+}
+// CFET6 row r (0-2), node j (0-4)
+__device__ __forceinline__ constexpr double hh(int r, int j) {
+  switch (r * 8 + j) {
+    case 0: return cfet::H11;  case 1: return cfet::H12;  case 2: return cfet::H13;
+    case 3: return cfet::H14;  case 4: return cfet::H15;
+    case 8: return cfet::H21;  case 9: return cfet::H22;  case 10: return cfet::H23;
+    case 11: return cfet::H24; case 12: return cfet::H25;
+    case 16: return cfet::H31; case 17: return cfet::H32; case 18: return cfet::H33;
+    case 19: return cfet::H34; default: return cfet::H35;
+  }
+}
+}  // namespace cfetc
+
+// v rotated by the angle |k| about -k/|k|: Rodrigues' formula
+// v cos + (v x k) sin/|k| + k (k.v)(1 - cos)/|k|^2 (rodriguez, src/quaternion.cpp).
+__device__ __forceinline__ void rodrigues(double kx, double ky, double kz, double& vx, double& vy, double& vz) {
+  const double a2 = fma(kz, kz, fma(ky, ky, kx * kx));
+  const double angle = sqrt(a2);
+  double s, c;
+  sincos(angle, &s, &c);
+  const double sa = s / angle;
+  const double d = fma(kz, vz, fma(ky, vy, kx * vx)) * (1.0 - c) / a2;
+  const double cx = fma(vy, kz, -vz * ky), cy = fma(vz, kx, -vx * kz), cz = fma(vx, ky, -vy * kx);
+  vx = fma(kx, d, fma(cx, sa, vx * c));
+  vy = fma(ky, d, fma(cy, sa, vy * c));
+  vz = fma(kz, d, fma(cz, sa, vz * c));
+}
+
+struct Quat {
+  double w, x, y, z;
+};
+
+// Rotation by the angle |k| dt about -k/|k| as a unit quaternion
+// (rodriguezQuat, src/quaternion.cpp).
+__device__ __forceinline__ Quat rot_quat(double kx, double ky, double kz, double dt) {
+  const double angle = sqrt(fma(kz, kz, fma(ky, ky, kx * kx)));
+  double s, c;
+  sincos(angle * dt * 0.5, &s, &c);
+  const double f = -s / angle;
+  return {c, kx * f, ky * f, kz * f};
+}
+
+// a b (qMult, src/quaternion.cpp)
+__device__ __forceinline__ Quat qmul(const Quat& a, const Quat& b) {
+  return {a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z, a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y,
+          a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z, a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x};
+}
+
+// q (0, v) q* (qv_mult, src/quaternion.cpp), the terms of the pure
+// quaternion's zero real part left out.
+__device__ __forceinline__ void qrotate(const Quat& q, double vx, double vy, double vz, double& ox, double& oy,
+                                        double& oz) {
+  const double tw = -(q.x * vx + q.y * vy + q.z * vz);
+  const double tx = q.w * vx + q.y * vz - q.z * vy;
+  const double ty = q.w * vy + q.z * vx - q.x * vz;
+  const double tz = q.w * vz + q.x * vy - q.y * vx;
+  // (tw, tx, ty, tz) (q.w, -q.x, -q.y, -q.z)
+  ox = -tw * q.x + tx * q.w - ty * q.z + tz * q.y;
+  oy = -tw * q.y + ty * q.w - tz * q.x + tx * q.z;
+  oz = -tw * q.z + tz * q.w - tx * q.y + ty * q.x;
+}
+
+// Magnus: the CFET8 product (exponents 11 down to 1, each h times a
+// combination of the field at the five Gauss-Legendre nodes) gives the
+// proposal, the CFET6 product beside it the error vector.
+__device__ __forceinline__ void magnus_stages(const Seg& g, const SetParams& P, double tx, double h, double Sx,
+                                              double Sy, double Sz, double w[3], double e[3]) {
+  double B[5][3];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) omega_at(g, P, fma(cfetc::x(i), h, tx), B[i][0], B[i][1], B[i][2]);
+  double y8[3] = {Sx, Sy, Sz}, y6[3] = {Sx, Sy, Sz};
+#pragma unroll
+  for (int n = 0; n < 11; ++n) {
+    // exponent 11 - n: rows 1..5 reversed, then rows 6..1
+    const int r = n < 5 ? n : 10 - n;
+    const bool rev = n < 5;
+    double k[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double s = cfetc::g(r, rev ? 4 : 0) * B[0][c];
+#pragma unroll
+      for (int j = 1; j < 5; ++j) s = fma(cfetc::g(r, rev ? 4 - j : j), B[j][c], s);
+      k[c] = h * s;
+    }
+    rodrigues(k[0], k[1], k[2], y8[0], y8[1], y8[2]);
+  }
+#pragma unroll
+  for (int n = 0; n < 5; ++n) {
+    // exponent 5 - n: rows 1, 2 reversed, then rows 3..1
+    const int r = n < 2 ? n : 4 - n;
+    const bool rev = n < 2;
+    double k[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double s = cfetc::hh(r, rev ? 4 : 0) * B[0][c];
+#pragma unroll
+      for (int j = 1; j < 5; ++j) s = fma(cfetc::hh(r, rev ? 4 - j : j), B[j][c], s);
+      k[c] = h * s;
+    }
+    rodrigues(k[0], k[1], k[2], y6[0], y6[1], y6[2]);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    w[c] = y8[c];
+    e[c] = y8[c] - y6[c];
+  }
+}
+
+// RK45 / RKF45 with quaternions: the field at the six nodes, each turned into
+// a rotation by h times a weight and composed; the proposal uses the six
+// higher-order weights (RK45: CH, RKF45: C1..C6), the comparison rotation the
+// first five lower-order ones (RK45: C1..C5; RKF45: its own C1..C5, so the
+// two products share all but the last factor).  Stage 2's weights are zero.
+template <bool F>
+__device__ __forceinline__ void quat_stages(const Seg& g, const SetParams& P, double tx, double h, double Sx,
+                                            double Sy, double Sz, double w[3], double e[3]) {
+  double Ox, Oy, Oz;
+  omega_at(g, P, tx, Ox, Oy, Oz);
+  Quat qw = rot_quat(Ox, Oy, Oz, h * (F ? rkf45::C1 : rk45::CH1));
+  Quat qe = F ? qw : rot_quat(Ox, Oy, Oz, h * rk45::C1);
+#pragma unroll
+  for (int s = 3; s <= 6; ++s) {
+    const double A = F ? (s == 3 ? rkf45::A3 : s == 4 ? rkf45::A4 : s == 5 ? rkf45::A5 : rkf45::A6)
+                       : (s == 3 ? rk45::A3 : s == 4 ? rk45::A4 : s == 5 ? rk45::A5 : rk45::A6);
+    omega_at(g, P, fma(A, h, tx), Ox, Oy, Oz);
+    if (F) {
+      const double W = s == 3 ? rkf45::C3 : s == 4 ? rkf45::C4 : s == 5 ? rkf45::C5 : rkf45::C6;
+      if (s < 6) {
+        qe = qmul(rot_quat(Ox, Oy, Oz, h * W), qe);
+        qw = qe;
+      } else {
+        qw = qmul(rot_quat(Ox, Oy, Oz, h * W), qe);
+      }
+    } else {
+      const double W = s == 3 ? rk45::CH3 : s == 4 ? rk45::CH4 : s == 5 ? rk45::CH5 : rk45::CH6;
+      qw = qmul(rot_quat(Ox, Oy, Oz, h * W), qw);
+      if (s < 6) {
+        const double E = s == 3 ? rk45::C3 : s == 4 ? rk45::C4 : rk45::C5;
+        qe = qmul(rot_quat(Ox, Oy, Oz, h * E), qe);
+      }
+    }
+  }
+  double cx, cy, cz;
+  qrotate(qw, Sx, Sy, Sz, w[0], w[1], w[2]);
+  qrotate(qe, Sx, Sy, Sz, cx, cy, cz);
+  e[0] = w[0] - cx;
+  e[1] = w[1] - cy;
+  e[2] = w[2] - cz;
+}
+
+// RKF45 with RK45's first-stage quirk (k1 at the previous attempt's last
+// stage state, kept in g.k); its error vector is h times the whole
+// fourth-order combination, as the reference computes it.
+__device__ __forceinline__ void rkf45_stages(Seg& g, const SetParams& P, double tx, double h, double Sx, double Sy,
+                                             double Sz, double w[3], double e[3]) {
+  using namespace rkf45;
+  double k1x, k1y, k1z, k2x, k2y, k2z, k3x, k3y, k3z, k4x, k4y, k4z, k5x, k5y, k5z, k6x, k6y, k6z;
+  double yx, yy, yz;
+  feval(g, P, tx, g.kx, g.ky, g.kz, k1x, k1y, k1z);
+  yx = fma(h * B21, k1x, Sx); yy = fma(h * B21, k1y, Sy); yz = fma(h * B21, k1z, Sz);
+  feval(g, P, fma(A2, h, tx), yx, yy, yz, k2x, k2y, k2z);
+  yx = fma(h, fma(B32, k2x, B31 * k1x), Sx);
+  yy = fma(h, fma(B32, k2y, B31 * k1y), Sy);
+  yz = fma(h, fma(B32, k2z, B31 * k1z), Sz);
+  feval(g, P, fma(A3, h, tx), yx, yy, yz, k3x, k3y, k3z);
+  yx = fma(h, fma(B43, k3x, fma(B42, k2x, B41 * k1x)), Sx);
+  yy = fma(h, fma(B43, k3y, fma(B42, k2y, B41 * k1y)), Sy);
+  yz = fma(h, fma(B43, k3z, fma(B42, k2z, B41 * k1z)), Sz);
+  feval(g, P, fma(A4, h, tx), yx, yy, yz, k4x, k4y, k4z);
+  yx = fma(h, fma(B54, k4x, fma(B53, k3x, fma(B52, k2x, B51 * k1x))), Sx);
+  yy = fma(h, fma(B54, k4y, fma(B53, k3y, fma(B52, k2y, B51 * k1y))), Sy);
+  yz = fma(h, fma(B54, k4z, fma(B53, k3z, fma(B52, k2z, B51 * k1z))), Sz);
+  feval(g, P, fma(A5, h, tx), yx, yy, yz, k5x, k5y, k5z);
+  yx = fma(h, fma(B65, k5x, fma(B64, k4x, fma(B63, k3x, fma(B62, k2x, B61 * k1x)))), Sx);
+  yy = fma(h, fma(B65, k5y, fma(B64, k4y, fma(B63, k3y, fma(B62, k2y, B61 * k1y)))), Sy);
+  yz = fma(h, fma(B65, k5z, fma(B64, k4z, fma(B63, k3z, fma(B62, k2z, B61 * k1z)))), Sz);
+  feval(g, P, fma(A6, h, tx), yx, yy, yz, k6x, k6y, k6z);
+  g.kx = yx; g.ky = yy; g.kz = yz;
+  w[0] = fma(h, fma(C6, k6x, fma(C5, k5x, fma(C4, k4x, fma(C3, k3x, C1 * k1x)))), Sx);
+  w[1] = fma(h, fma(C6, k6y, fma(C5, k5y, fma(C4, k4y, fma(C3, k3y, C1 * k1y)))), Sy);
+  w[2] = fma(h, fma(C6, k6z, fma(C5, k5z, fma(C4, k4z, fma(C3, k3z, C1 * k1z)))), Sz);
+  e[0] = h * fma(CR5, k5x, fma(CR4, k4x, fma(CR3, k3x, CR1 * k1x)));
+  e[1] = h * fma(CR5, k5y, fma(CR4, k4y, fma(CR3, k3y, CR1 * k1y)));
+  e[2] = h * fma(CR5, k5z, fma(CR4, k4z, fma(CR3, k3z, CR1 * k1z)));
+}
+
+// Start a type 2-5 call over the segment: the same state as RK45's.
+__device__ __forceinline__ void ext_begin(Seg& g, double h) { rk45_begin(g, h); }
+
+// One attempt of integrator type 2-5 (P.integrator).  Their shared step
+// controller differs from RK45's: the segment end is tested before the hmax
+// and hmin limits, and a fixed step never looks at the segment end (such a
+// segment ends after nmax attempts, -2).  Returns 0 to continue, 1 at the
+// segment end (g.h then holds the carried step), -1 when h < hmin, -2 after
+// more than nmax attempts.
+__device__ __forceinline__ int ext_attempt(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz) {
+  g.nstep++;
+  if (g.nstep > P.nmax) return -2;
+  const double endDt = g.xf - g.x;
+  double h = g.h;
+  g.lastH = h;
+  bool stop = false;
+  if (P.fixed) {
+    h = P.h0;
+  } else if (h >= endDt) {
+    h = endDt;
+    stop = true;
+  } else if (h > P.hmax) {
+    h = std_min(h, P.hmax);
+  } else if (h < P.hmin) {
+    return -1;
+  }
+  const double tx = g.x - g.t0;
+  double w[3], e[3];
+  if (P.integrator == 2)
+    magnus_stages(g, P, tx, h, Sx, Sy, Sz, w, e);
+  else if (P.integrator == 3)
+    quat_stages<false>(g, P, tx, h, Sx, Sy, Sz, w, e);
+  else if (P.integrator == 5)
+    quat_stages<true>(g, P, tx, h, Sx, Sy, Sz, w, e);
+  else
+    rkf45_stages(g, P, tx, h, Sx, Sy, Sz, w, e);
+  double error = sqrt(fma(e[2], e[2], fma(e[1], e[1], e[0] * e[0])));
+  error = std_max(error, 1.0e-16);
+  const double ratio = P.rtol / error;
+  const double lnr = log(ratio);
+  double q = exp(rk45::E1 * lnr + rk45::E2 * g.lnprev);  // ratio^E1 * prev_ratio^E2
+  q = std_min(q, 4.0);
+  if ((q > 0.81 && error < 2.0 * P.rtol) || P.fixed) {
+    g.turns += count_turn(Sy, Sz, w[1], w[2]);
+    Sx = w[0]; Sy = w[1]; Sz = w[2];
     g.x += h;
     if (stop) {
       g.h = g.lastH;

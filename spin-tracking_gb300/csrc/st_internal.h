@@ -40,7 +40,8 @@ struct SetParams {
   double t0, tf, ioutInt;
   double yi_x, yi_y, yi_z;
   unsigned int nmax, seed;
-  int integrator;                 // 0 DOP853, 1 RK45, any other value: trajectory only
+  int integrator;                 // 0 DOP853, 1 RK45, 2 Magnus CFET8, 3 RK45 with quaternions,
+                                  // 4 RKF45, 5 RKF45 with quaternions; other values: trajectory only
   int nwin;                       // floor((tf - t0) / ioutInt)
   int gravity, gas, fixed, keep;
   int dist;                       // 'C' or 'M'
@@ -78,6 +79,7 @@ struct RunStatus {
   unsigned long long dop_attempts;
   unsigned long long rk45_attempts;
   unsigned long long segments;
+  unsigned long long ext_attempts;  // step attempts of integrator types 2-5
   unsigned long long queue_head;   // persistent-kernel work queue cursor
   unsigned long long deadline_ns;  // %globaltimer value after which lanes stop (0 = none)
   int deadline_hit;
@@ -97,6 +99,7 @@ struct RunArgs {
   int deadline_armed;             // read RunStatus::deadline_ns at kernel start
   int count_work;                 // accumulate attempt counters
   int any_gas;                    // some set has gas collisions (else gas-free kernels may run)
+  int any_ext;                    // some set integrates with type 2-5 (the EXT kernels must run)
 };
 
 // Discrete adjoint (st_adjoint.cu): gradient of L(S_final) with respect to
@@ -175,7 +178,7 @@ int persistent_variant_count();
 // Host helpers shared across the library's translation units.
 int build_set_params(const st_options& o, int64_t first, SetParams* P);
 int set_last_error(int code, const char* msg);
-int persistent_max_blocks_per_sm(int variant, int block);
+int persistent_max_blocks_per_sm(int variant, int ext);  // ext: the integrator type 2-5 kernel
 int persistent_prepare(int variant);
 int persistent_variant_block(int variant);
 const char* persistent_variant_name(int variant);

@@ -169,6 +169,8 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
   a.deadline_armed = 0;
   a.count_work = 1;
   a.any_gas = 1;  // the caller's sets are not inspected on the host: the kernel with gas handles any set
+  a.any_ext = 0;
+  for (int k = 0; k < nsets; ++k) a.any_ext |= (sets[k].integratorType >= 2 && sets[k].integratorType <= 5) ? 1 : 0;
   if (int pe = launch_prepare_sets(params, nsets, st_)) return set_last_error(ST_ERR_CUDA, cudaGetErrorString((cudaError_t)pe));
   if (n > 0) {
     k_noalloc_sets<<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(a.s, params, nsets);

@@ -71,7 +71,8 @@ class Ensemble(ctypes.Structure):
 
 class Counters(ctypes.Structure):
     _fields_ = [("dop_attempts", c_uint64), ("rk45_attempts", c_uint64), ("segments", c_uint64),
-                ("kernel_launches", c_uint64), ("graph_launches", c_uint64), ("graph_captures", c_uint64)]
+                ("kernel_launches", c_uint64), ("graph_launches", c_uint64), ("graph_captures", c_uint64),
+                ("ext_attempts", c_uint64)]
 
 
 ST_OK = 0

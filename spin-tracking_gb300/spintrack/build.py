@@ -22,7 +22,7 @@ CLI = BUILD / "spintrack"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
-UNITS = ["st_kernels.cu", "st_api.cpp", "st_noalloc.cu", "st_adjoint.cu", "st_ensemble.cu"]
+UNITS = ["st_kernels.cu", "st_kernels_ext.cu", "st_api.cpp", "st_noalloc.cu", "st_adjoint.cu", "st_ensemble.cu"]
 
 
 def _nvcc() -> str:

@@ -127,8 +127,7 @@ def test_writer_layout(stlib, tmp_path):
     assert len(snaps) == 1 and np.array_equal(snaps[0]["n_steps"], ns) and np.array_equal(snaps[0]["S"], S)
 
 
-@pytest.mark.parametrize("field,value,code", [("integratorType", 2, _capi.ST_ERR_UNSUPPORTED),
-                                              ("integratorType", 6, _capi.ST_ERR_UNSUPPORTED),
+@pytest.mark.parametrize("field,value,code", [("integratorType", 6, _capi.ST_ERR_UNSUPPORTED),
                                               ("dist", b"X", _capi.ST_ERR_UNSUPPORTED),
                                               ("ioutInt", 0.0, _capi.ST_ERR_ARG),
                                               ("numParticles", -1, _capi.ST_ERR_ARG)])
