@@ -251,6 +251,12 @@ WORKLOADS = {
                      "4.2 K, specular walls, gravity, gas off, G ~ N(0,1e-9) T/m, E = (0,0,75e5), B0 = (3e-6,0,0), "
                      "tf = 0.05 s, tape pool 3 GB (the tape, ~0.9 GB, stays resident); gradients of <Sx>, <Sy> and "
                      "the mean precession phase",
+    "integrators": "the six integrator types on the headline physics (65,536 particles, MB 4.2 K, diffuse 0.1, "
+                   "gravity, full G, E = (0,0,75e5), B0 = (3e-6,0,0), gas off): DOP853 rtol 1e-12 tf 0.2 s, RK45 "
+                   "rtol 1e-12 tf 2e-4 s, Magnus CFET8 rtol 1e-12 tf 0.2 s, RK45 with quaternions rtol 1e-10 tf "
+                   "0.05 s, RKF45 rtol 1e-3 tf 0.02 s, RKF45 with quaternions rtol 1e-6 tf 1e-3 s (the RKF45 "
+                   "pair's error estimates are the whole increment and the last stage's rotation: they accept "
+                   "only steps of ~3 us and ~0.1 us, and tighter tolerances fail with h < hmin), one window each",
     "dressing-grid": "dressing sensitivity: 8 x 8 grid a in [1,10] uT, w in 2 pi [500,2000] rad/s as 64 parameter "
                      "sets x 4096 particles in one context, otherwise as 'dressing' with tf = 0.2 s; d<P>/d(a, w) of "
                      "the polarisation P = |<S>| per grid point from one record + one backward pass",
@@ -320,9 +326,29 @@ def run_workload(args):
     line = {"workload": args.workload, "description": WORKLOADS[args.workload], "n_gpus": 1, "dtype": "f64",
             "data": "synthetic"}
 
-    def roofline(counters, secs):
-        ach = workmodel.algorithmic_flops(counters) / secs / 1e12
+    def roofline(counters, secs, ext_type=None):
+        ach = workmodel.algorithmic_flops(counters, ext_type) / secs / 1e12
         return {"bound": "fp64", "achieved": ach, "peak": peak.value, "unit": "TFLOP/s", "frac": ach / peak.value}
+
+    if args.workload == "integrators":
+        names = {0: "DOP853", 1: "RK45", 2: "Magnus CFET8", 3: "RK45 quaternion", 4: "RKF45", 5: "RKF45 quaternion"}
+        plan = ((0, 1e-12, 0.2), (1, 1e-12, 2e-4), (2, 1e-12, 0.2), (3, 1e-10, 0.05), (4, 1e-3, 0.02), (5, 1e-6, 1e-3))
+        per = []
+        for it, rtol, tf in plan:
+            o = _set_options(65536, tf, integratorType=it, rtol=rtol, ioutInt=tf)
+            with st.Particles(o, device=dev) as p:
+                secs, clk = _timed_forward(p, 1, args.steps, 1, dev)
+                c = p.counters()
+                att = c["dop_attempts"] + c["rk45_attempts"] + c["ext_attempts"]
+                per.append({"integratorType": it, "name": names[it], "rtol": rtol, "tf": tf,
+                            "value": 65536 * tf / secs, "ms_per_step": secs * 1e3, "attempts": att,
+                            "attempts_per_s": att / secs, "segments": c["segments"],
+                            "failed": int(np.count_nonzero(p.output_data()["fail"])),
+                            "roofline": roofline(c, secs, it if it >= 2 else None),
+                            "launch_config": list(p.launch_config()), "clocks": clk})
+        line.update({"metric": "particle*s simulated/s per integrator type", "unit": "particle*s/s",
+                     "steps": args.steps, "warmup": 1, "per_type": per})
+        return line
 
     if args.workload in ("sweep", "dressing", "literal-gas"):
         if args.workload == "sweep":

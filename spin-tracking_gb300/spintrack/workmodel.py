@@ -22,12 +22,26 @@ RK45 attempt (rk45_attempt): 6 field + Bloch evaluations (132), stage
 Trajectory segment (traj_event + seg_setup + dop_begin): wall times (~20),
   ballistic move and speed (~30), checks (~5), field polynomial setup (~75),
   first derivative (21)                                             150
+Integrator types 2-5 (ext_attempt; sincos of the rotations not counted):
+  Magnus CFET8: 5 node fields (70), 16 exponents h sum c_j B_j (480),
+    16 Rodrigues rotations (39 each: 624), error and controller (34)  1208
+  RK45 with quaternions: 5 node fields (68), 9 rotation quaternions (117),
+    7 quaternion products (196), 2 rotations q (0,S) q* (82), error and
+    controller (34)                                                   497
+  RKF45: as RK45                                                      318
+  RKF45 with quaternions: 5 node fields (68), 5 rotation quaternions (65),
+    4 products (112), 2 rotations (82), error and controller (34)     361
 """
 FLOPS_PER_DOP_ATTEMPT = 785
 FLOPS_PER_RK45_ATTEMPT = 318
 FLOPS_PER_SEGMENT = 150
+FLOPS_PER_EXT_ATTEMPT = {2: 1208, 3: 497, 4: 318, 5: 361}
 
 
-def algorithmic_flops(counters: dict) -> float:
+def algorithmic_flops(counters: dict, ext_type: int | None = None) -> float:
+    """FP64 work of a run's counted attempts; ext_type names the one type 2-5
+    behind counters["ext_attempts"] (a run mixing several has no single
+    figure for them: their attempts are then left out)."""
+    ext = counters.get("ext_attempts", 0) * FLOPS_PER_EXT_ATTEMPT.get(ext_type, 0) if ext_type else 0
     return (counters["dop_attempts"] * FLOPS_PER_DOP_ATTEMPT + counters["rk45_attempts"] * FLOPS_PER_RK45_ATTEMPT
-            + counters["segments"] * FLOPS_PER_SEGMENT)
+            + counters["segments"] * FLOPS_PER_SEGMENT + ext)
