@@ -334,14 +334,20 @@ def run_workload(args):
         names = {0: "DOP853", 1: "RK45", 2: "Magnus CFET8", 3: "RK45 quaternion", 4: "RKF45", 5: "RKF45 quaternion"}
         plan = ((0, 1e-12, 0.2), (1, 1e-12, 2e-4), (2, 1e-12, 0.2), (3, 1e-10, 0.05), (4, 1e-3, 0.02), (5, 1e-6, 1e-3))
         per = []
+        want = {int(x) for x in args.types.split(",") if x.strip()}
+        npt = args.type_particles
         for it, rtol, tf in plan:
-            o = _set_options(65536, tf, integratorType=it, rtol=rtol, ioutInt=tf)
+            if it not in want:
+                continue
+            o = _set_options(npt, tf, integratorType=it, rtol=rtol, ioutInt=tf)
             with st.Particles(o, device=dev) as p:
+                if args.variant >= 0:
+                    p.set_launch_config(args.variant, args.bps)
                 secs, clk = _timed_forward(p, 1, args.steps, 1, dev)
                 c = p.counters()
                 att = c["dop_attempts"] + c["rk45_attempts"] + c["ext_attempts"]
                 per.append({"integratorType": it, "name": names[it], "rtol": rtol, "tf": tf,
-                            "value": 65536 * tf / secs, "ms_per_step": secs * 1e3, "attempts": att,
+                            "particles": npt, "value": npt * tf / secs, "ms_per_step": secs * 1e3, "attempts": att,
                             "attempts_per_s": att / secs, "segments": c["segments"],
                             "failed": int(np.count_nonzero(p.output_data()["fail"])),
                             "roofline": roofline(c, secs, it if it >= 2 else None),
@@ -650,6 +656,10 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=None,
                     help="print the line of one additional configuration instead of the headline line")
+    ap.add_argument("--types", type=str, default="0,1,2,3,4,5",
+                    help="integrator types of the 'integrators' workload (comma-separated)")
+    ap.add_argument("--type-particles", type=int, default=65536,
+                    help="particles per integrator type in the 'integrators' workload")
     args = ap.parse_args()
     if args.workload:
         print(json.dumps(run_workload(args)), flush=True)

@@ -1000,13 +1000,16 @@ __device__ __forceinline__ constexpr double hh(int r, int j) {
 
 // v rotated by the angle |k| about -k/|k|: Rodrigues' formula
 // v cos + (v x k) sin/|k| + k (k.v)(1 - cos)/|k|^2 (rodriguez, src/quaternion.cpp).
+// One reciprocal square root gives |k|, 1/|k| and 1/|k|^2 (the reference
+// takes a square root and two divisions).
 __device__ __forceinline__ void rodrigues(double kx, double ky, double kz, double& vx, double& vy, double& vz) {
   const double a2 = fma(kz, kz, fma(ky, ky, kx * kx));
-  const double angle = sqrt(a2);
+  const double r = rsqrt(a2);
+  const double angle = a2 * r;
   double s, c;
   sincos(angle, &s, &c);
-  const double sa = s / angle;
-  const double d = fma(kz, vz, fma(ky, vy, kx * vx)) * (1.0 - c) / a2;
+  const double sa = s * r;
+  const double d = fma(kz, vz, fma(ky, vy, kx * vx)) * (1.0 - c) * (r * r);
   const double cx = fma(vy, kz, -vz * ky), cy = fma(vz, kx, -vx * kz), cz = fma(vx, ky, -vy * kx);
   vx = fma(kx, d, fma(cx, sa, vx * c));
   vy = fma(ky, d, fma(cy, sa, vy * c));
@@ -1020,10 +1023,11 @@ struct Quat {
 // Rotation by the angle |k| dt about -k/|k| as a unit quaternion
 // (rodriguezQuat, src/quaternion.cpp).
 __device__ __forceinline__ Quat rot_quat(double kx, double ky, double kz, double dt) {
-  const double angle = sqrt(fma(kz, kz, fma(ky, ky, kx * kx)));
+  const double a2 = fma(kz, kz, fma(ky, ky, kx * kx));
+  const double r = rsqrt(a2);
   double s, c;
-  sincos(angle * dt * 0.5, &s, &c);
-  const double f = -s / angle;
+  sincos(a2 * r * dt * 0.5, &s, &c);
+  const double f = -s * r;
   return {c, kx * f, ky * f, kz * f};
 }
 
@@ -1052,9 +1056,13 @@ __device__ __forceinline__ void qrotate(const Quat& q, double vx, double vy, dou
 // proposal, the CFET6 product beside it the error vector.
 __device__ __forceinline__ void magnus_stages(const Seg& g, const SetParams& P, double tx, double h, double Sx,
                                               double Sy, double Sz, double w[3], double e[3]) {
-  double B[5][3];
+  double B[5][3];  // h Omega at the nodes: the exponents are combinations of these
 #pragma unroll
-  for (int i = 0; i < 5; ++i) omega_at(g, P, fma(cfetc::x(i), h, tx), B[i][0], B[i][1], B[i][2]);
+  for (int i = 0; i < 5; ++i) {
+    omega_at(g, P, fma(cfetc::x(i), h, tx), B[i][0], B[i][1], B[i][2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B[i][c] *= h;
+  }
   double y8[3] = {Sx, Sy, Sz}, y6[3] = {Sx, Sy, Sz};
 #pragma unroll
   for (int n = 0; n < 11; ++n) {
@@ -1067,7 +1075,7 @@ __device__ __forceinline__ void magnus_stages(const Seg& g, const SetParams& P, 
       double s = cfetc::g(r, rev ? 4 : 0) * B[0][c];
 #pragma unroll
       for (int j = 1; j < 5; ++j) s = fma(cfetc::g(r, rev ? 4 - j : j), B[j][c], s);
-      k[c] = h * s;
+      k[c] = s;
     }
     rodrigues(k[0], k[1], k[2], y8[0], y8[1], y8[2]);
   }
@@ -1082,7 +1090,7 @@ __device__ __forceinline__ void magnus_stages(const Seg& g, const SetParams& P, 
       double s = cfetc::hh(r, rev ? 4 : 0) * B[0][c];
 #pragma unroll
       for (int j = 1; j < 5; ++j) s = fma(cfetc::hh(r, rev ? 4 - j : j), B[j][c], s);
-      k[c] = h * s;
+      k[c] = s;
     }
     rodrigues(k[0], k[1], k[2], y6[0], y6[1], y6[2]);
   }

@@ -23,8 +23,9 @@ Trajectory segment (traj_event + seg_setup + dop_begin): wall times (~20),
   ballistic move and speed (~30), checks (~5), field polynomial setup (~75),
   first derivative (21)                                             150
 Integrator types 2-5 (ext_attempt; sincos of the rotations not counted):
-  Magnus CFET8: 5 node fields (70), 16 exponents h sum c_j B_j (480),
-    16 Rodrigues rotations (39 each: 624), error and controller (34)  1208
+  Magnus CFET8: 5 node fields (70) scaled by h (15), 16 exponents
+    sum c_j h B_j (432), 16 Rodrigues rotations (40 each: 640), error and
+    controller (34)                                                   1191
   RK45 with quaternions: 5 node fields (68), 9 rotation quaternions (117),
     7 quaternion products (196), 2 rotations q (0,S) q* (82), error and
     controller (34)                                                   497
@@ -35,7 +36,7 @@ Integrator types 2-5 (ext_attempt; sincos of the rotations not counted):
 FLOPS_PER_DOP_ATTEMPT = 785
 FLOPS_PER_RK45_ATTEMPT = 318
 FLOPS_PER_SEGMENT = 150
-FLOPS_PER_EXT_ATTEMPT = {2: 1208, 3: 497, 4: 318, 5: 361}
+FLOPS_PER_EXT_ATTEMPT = {2: 1191, 3: 497, 4: 318, 5: 361}
 
 
 def algorithmic_flops(counters: dict, ext_type: int | None = None) -> float:

@@ -2,7 +2,8 @@
 cleanly with ST_ERR_DEADLINE (lanes check %globaltimer, no kernel spins on
 anything), the context stays usable, and calling again resumes from the
 particles' last window-end checkpoints: the final state equals an
-uninterrupted run's bit for bit, for both kernels."""
+uninterrupted run's bit for bit, for both kernels, with DOP853 and with the
+Magnus stepper (whose kernels are the integrator type 2-5 instantiations)."""
 from __future__ import annotations
 
 import numpy as np
@@ -14,15 +15,16 @@ from spintrack._capi import ST_ERR_DEADLINE
 pytestmark = pytest.mark.gpu
 
 
-def deadline_options():
+def deadline_options(integrator=0):
     return st.derive(st.make_options(numParticles=4096, dist="M", T=4.2, diffuse=0.1, gas_coll=False, gravity=True,
                                      Gx=(0.0, 0.0, 1e-9), E=(0.0, 0.0, 75e5), yi=(0.0, 0.0, 1.0), tf=0.2,
-                                     ioutInt=0.05, seed=17))
+                                     ioutInt=0.05, seed=17, integratorType=integrator))
 
 
+@pytest.mark.parametrize("integrator", [0, 2], ids=["dop853", "magnus"])
 @pytest.mark.parametrize("kernel", [st.KERNEL_PERSISTENT, st.KERNEL_PLAIN], ids=["persistent", "plain"])
-def test_deadline_stops_and_the_next_call_resumes(gpu, kernel):
-    opt = deadline_options()
+def test_deadline_stops_and_the_next_call_resumes(gpu, kernel, integrator):
+    opt = deadline_options(integrator)
     nw = st.num_windows(opt)
     with st.Particles(opt) as p:
         p.init_particles()

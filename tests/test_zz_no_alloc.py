@@ -25,10 +25,8 @@ from spintrack import _capi
 pytestmark = pytest.mark.gpu
 
 
-def _sets():
-    a = st.derive(st.parse_params(GOLDEN / "m04_gas.params"))
-    b = st.derive(st.parse_params(GOLDEN / "c1_precess.params"))
-    return [a, b]
+def _sets(names=("m04_gas", "c1_precess")):
+    return [st.derive(st.parse_params(GOLDEN / f"{c}.params")) for c in names]
 
 
 def _reference(sets, nwin):
@@ -65,10 +63,12 @@ def _close(got, ref):
         assert np.all(np.abs(a[m] - b[m]) <= tol * np.maximum(1.0, np.abs(b[m]))), f
 
 
-def test_noalloc_matches_allocating_path_twice(gpu):
+@pytest.mark.parametrize("names", [("m04_gas", "c1_precess"), ("magnus", "rkf45q", "rk45")],
+                         ids=["dop853", "types-2-5"])
+def test_noalloc_matches_allocating_path_twice(gpu, names):
     import torch
     lib = _capi.load()
-    sets = _sets()
+    sets = _sets(names)
     nwin = min(st.num_windows(s) for s in sets)
     n = sum(int(s.numParticles) for s in sets)
     arr = (st.Options * len(sets))(*sets)
