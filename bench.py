@@ -251,10 +251,10 @@ WORKLOADS = {
                      "4.2 K, specular walls, gravity, gas off, G ~ N(0,1e-9) T/m, E = (0,0,75e5), B0 = (3e-6,0,0), "
                      "tf = 0.05 s, tape pool 3 GB (the tape, ~0.9 GB, stays resident); gradients of <Sx>, <Sy> and "
                      "the mean precession phase",
-    "integrators": "the six integrator types on the headline physics (65,536 particles, MB 4.2 K, diffuse 0.1, "
-                   "gravity, full G, E = (0,0,75e5), B0 = (3e-6,0,0), gas off): DOP853 rtol 1e-12 tf 0.2 s, RK45 "
-                   "rtol 1e-12 tf 2e-4 s, Magnus CFET8 rtol 1e-12 tf 0.2 s, RK45 with quaternions rtol 1e-10 tf "
-                   "0.05 s, RKF45 rtol 1e-3 tf 0.02 s, RKF45 with quaternions rtol 1e-6 tf 1e-3 s (the RKF45 "
+    "integrators": "the six integrator types on the headline physics (262,144 particles, MB 4.2 K, diffuse 0.1, "
+                   "gravity, full G, E = (0,0,75e5), B0 = (3e-6,0,0), gas off): DOP853 rtol 1e-12 tf 0.05 s, RK45 "
+                   "rtol 1e-12 tf 5e-5 s, Magnus CFET8 rtol 1e-12 tf 0.05 s, RK45 with quaternions rtol 1e-10 tf "
+                   "0.0125 s, RKF45 rtol 1e-3 tf 0.005 s, RKF45 with quaternions rtol 1e-6 tf 2.5e-4 s (the RKF45 "
                    "pair's error estimates are the whole increment and the last stage's rotation: they accept "
                    "only steps of ~3 us and ~0.1 us, and tighter tolerances fail with h < hmin), one window each",
     "dressing-grid": "dressing sensitivity: 8 x 8 grid a in [1,10] uT, w in 2 pi [500,2000] rad/s as 64 parameter "
@@ -332,7 +332,8 @@ def run_workload(args):
 
     if args.workload == "integrators":
         names = {0: "DOP853", 1: "RK45", 2: "Magnus CFET8", 3: "RK45 quaternion", 4: "RKF45", 5: "RKF45 quaternion"}
-        plan = ((0, 1e-12, 0.2), (1, 1e-12, 2e-4), (2, 1e-12, 0.2), (3, 1e-10, 0.05), (4, 1e-3, 0.02), (5, 1e-6, 1e-3))
+        plan = ((0, 1e-12, 0.05), (1, 1e-12, 5e-5), (2, 1e-12, 0.05), (3, 1e-10, 0.0125), (4, 1e-3, 0.005),
+                (5, 1e-6, 2.5e-4))
         per = []
         want = {int(x) for x in args.types.split(",") if x.strip()}
         npt = args.type_particles
@@ -658,7 +659,7 @@ def main():
                     help="print the line of one additional configuration instead of the headline line")
     ap.add_argument("--types", type=str, default="0,1,2,3,4,5",
                     help="integrator types of the 'integrators' workload (comma-separated)")
-    ap.add_argument("--type-particles", type=int, default=65536,
+    ap.add_argument("--type-particles", type=int, default=262144,
                     help="particles per integrator type in the 'integrators' workload")
     args = ap.parse_args()
     if args.workload:

@@ -1051,9 +1051,30 @@ __device__ __forceinline__ void qrotate(const Quat& q, double vx, double vy, dou
   oz = -tw * q.z + tz * q.w - tx * q.y + ty * q.x;
 }
 
-// Magnus: the CFET8 product (exponents 11 down to 1, each h times a
-// combination of the field at the five Gauss-Legendre nodes) gives the
-// proposal, the CFET6 product beside it the error vector.
+// The Magnus stepper's 16 exponents in the order they are applied: the
+// CFET8 exponents 11 down to 1 (rows 1..5 with the node order reversed, then
+// rows 6..1), then the CFET6 exponents 5 down to 1 (rows 1, 2 reversed, then
+// rows 3..1); entry [n][j] weights the field at node j.  The stepper reads
+// them in a rolled loop, so the rotation code (with its sincos) appears once
+// in the kernel instead of 16 times: the unrolled form stalled on
+// instruction fetch.
+constexpr int magnus_row(int n) { return n < 5 ? n : (n < 11 ? 10 - n : (n < 13 ? n - 11 : 15 - n)); }
+constexpr bool magnus_rev(int n) { return n < 5 || n == 11 || n == 12; }
+#define ST_MAGNUS_ROW(n)                                                                                      \
+  {n < 11 ? cfetc::g(magnus_row(n), magnus_rev(n) ? 4 : 0) : cfetc::hh(magnus_row(n), magnus_rev(n) ? 4 : 0), \
+   n < 11 ? cfetc::g(magnus_row(n), magnus_rev(n) ? 3 : 1) : cfetc::hh(magnus_row(n), magnus_rev(n) ? 3 : 1), \
+   n < 11 ? cfetc::g(magnus_row(n), 2) : cfetc::hh(magnus_row(n), 2),                                        \
+   n < 11 ? cfetc::g(magnus_row(n), magnus_rev(n) ? 1 : 3) : cfetc::hh(magnus_row(n), magnus_rev(n) ? 1 : 3), \
+   n < 11 ? cfetc::g(magnus_row(n), magnus_rev(n) ? 0 : 4) : cfetc::hh(magnus_row(n), magnus_rev(n) ? 0 : 4)}
+static __constant__ double kMagnusExp[16][5] = {
+    ST_MAGNUS_ROW(0),  ST_MAGNUS_ROW(1),  ST_MAGNUS_ROW(2),  ST_MAGNUS_ROW(3),  ST_MAGNUS_ROW(4),  ST_MAGNUS_ROW(5),
+    ST_MAGNUS_ROW(6),  ST_MAGNUS_ROW(7),  ST_MAGNUS_ROW(8),  ST_MAGNUS_ROW(9),  ST_MAGNUS_ROW(10), ST_MAGNUS_ROW(11),
+    ST_MAGNUS_ROW(12), ST_MAGNUS_ROW(13), ST_MAGNUS_ROW(14), ST_MAGNUS_ROW(15)};
+#undef ST_MAGNUS_ROW
+
+// Magnus: the CFET8 product (exponents 11 down to 1, each a combination of h
+// times the field at the five Gauss-Legendre nodes) gives the proposal, the
+// CFET6 product beside it the error vector.
 __device__ __forceinline__ void magnus_stages(const Seg& g, const SetParams& P, double tx, double h, double Sx,
                                               double Sy, double Sz, double w[3], double e[3]) {
   double B[5][3];  // h Omega at the nodes: the exponents are combinations of these
@@ -1063,76 +1084,67 @@ __device__ __forceinline__ void magnus_stages(const Seg& g, const SetParams& P, 
 #pragma unroll
     for (int c = 0; c < 3; ++c) B[i][c] *= h;
   }
-  double y8[3] = {Sx, Sy, Sz}, y6[3] = {Sx, Sy, Sz};
+  double y[3] = {Sx, Sy, Sz}, y8[3];
+#pragma unroll 1
+  for (int n = 0; n < 16; ++n) {
+    if (n == 11) {  // CFET8 done: start CFET6 from S
 #pragma unroll
-  for (int n = 0; n < 11; ++n) {
-    // exponent 11 - n: rows 1..5 reversed, then rows 6..1
-    const int r = n < 5 ? n : 10 - n;
-    const bool rev = n < 5;
+      for (int c = 0; c < 3; ++c) {
+        y8[c] = y[c];
+        y[c] = c == 0 ? Sx : (c == 1 ? Sy : Sz);
+      }
+    }
+    const double* cf = kMagnusExp[n];
     double k[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      double s = cfetc::g(r, rev ? 4 : 0) * B[0][c];
+      double s = cf[0] * B[0][c];
 #pragma unroll
-      for (int j = 1; j < 5; ++j) s = fma(cfetc::g(r, rev ? 4 - j : j), B[j][c], s);
+      for (int j = 1; j < 5; ++j) s = fma(cf[j], B[j][c], s);
       k[c] = s;
     }
-    rodrigues(k[0], k[1], k[2], y8[0], y8[1], y8[2]);
-  }
-#pragma unroll
-  for (int n = 0; n < 5; ++n) {
-    // exponent 5 - n: rows 1, 2 reversed, then rows 3..1
-    const int r = n < 2 ? n : 4 - n;
-    const bool rev = n < 2;
-    double k[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      double s = cfetc::hh(r, rev ? 4 : 0) * B[0][c];
-#pragma unroll
-      for (int j = 1; j < 5; ++j) s = fma(cfetc::hh(r, rev ? 4 - j : j), B[j][c], s);
-      k[c] = s;
-    }
-    rodrigues(k[0], k[1], k[2], y6[0], y6[1], y6[2]);
+    rodrigues(k[0], k[1], k[2], y[0], y[1], y[2]);
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     w[c] = y8[c];
-    e[c] = y8[c] - y6[c];
+    e[c] = y8[c] - y[c];
   }
 }
 
-// RK45 / RKF45 with quaternions: the field at the six nodes, each turned into
-// a rotation by h times a weight and composed; the proposal uses the six
-// higher-order weights (RK45: CH, RKF45: C1..C6), the comparison rotation the
-// first five lower-order ones (RK45: C1..C5; RKF45: its own C1..C5, so the
-// two products share all but the last factor).  Stage 2's weights are zero.
+// Per stage m (stages 1, 3, 4, 5, 6; stage 2's weights are zero): node,
+// weight of the proposal's rotation, weight of the comparison's (RK45 only).
+static __constant__ double kQuatStages[2][5][3] = {
+    {{0.0, rk45::CH1, rk45::C1}, {rk45::A3, rk45::CH3, rk45::C3}, {rk45::A4, rk45::CH4, rk45::C4},
+     {rk45::A5, rk45::CH5, rk45::C5}, {rk45::A6, rk45::CH6, 0.0}},
+    {{0.0, rkf45::C1, 0.0}, {rkf45::A3, rkf45::C3, 0.0}, {rkf45::A4, rkf45::C4, 0.0}, {rkf45::A5, rkf45::C5, 0.0},
+     {rkf45::A6, rkf45::C6, 0.0}}};
+
+// RK45 / RKF45 with quaternions: the field at the stages' nodes, each turned
+// into a rotation by h times a weight and composed (the first factor onto the
+// identity, which is exact); the proposal uses the higher-order weights
+// (RK45: CH1..CH6, RKF45: C1..C6), the comparison rotation the first five
+// lower-order ones (RK45: C1..C5; RKF45: its own C1..C5, so the two products
+// share all but the last factor).  A rolled loop keeps one copy of the
+// rotation code in the kernel.
 template <bool F>
 __device__ __forceinline__ void quat_stages(const Seg& g, const SetParams& P, double tx, double h, double Sx,
                                             double Sy, double Sz, double w[3], double e[3]) {
-  double Ox, Oy, Oz;
-  omega_at(g, P, tx, Ox, Oy, Oz);
-  Quat qw = rot_quat(Ox, Oy, Oz, h * (F ? rkf45::C1 : rk45::CH1));
-  Quat qe = F ? qw : rot_quat(Ox, Oy, Oz, h * rk45::C1);
-#pragma unroll
-  for (int s = 3; s <= 6; ++s) {
-    const double A = F ? (s == 3 ? rkf45::A3 : s == 4 ? rkf45::A4 : s == 5 ? rkf45::A5 : rkf45::A6)
-                       : (s == 3 ? rk45::A3 : s == 4 ? rk45::A4 : s == 5 ? rk45::A5 : rk45::A6);
-    omega_at(g, P, fma(A, h, tx), Ox, Oy, Oz);
+  Quat qw = {1.0, 0.0, 0.0, 0.0}, qe = {1.0, 0.0, 0.0, 0.0};
+#pragma unroll 1
+  for (int m = 0; m < 5; ++m) {
+    const double* cf = kQuatStages[F ? 1 : 0][m];
+    double Ox, Oy, Oz;
+    omega_at(g, P, fma(cf[0], h, tx), Ox, Oy, Oz);
     if (F) {
-      const double W = s == 3 ? rkf45::C3 : s == 4 ? rkf45::C4 : s == 5 ? rkf45::C5 : rkf45::C6;
-      if (s < 6) {
-        qe = qmul(rot_quat(Ox, Oy, Oz, h * W), qe);
-        qw = qe;
-      } else {
-        qw = qmul(rot_quat(Ox, Oy, Oz, h * W), qe);
-      }
+      const Quat r = rot_quat(Ox, Oy, Oz, h * cf[1]);
+      if (m < 4)
+        qe = qmul(r, qe);
+      else
+        qw = qmul(r, qe);
     } else {
-      const double W = s == 3 ? rk45::CH3 : s == 4 ? rk45::CH4 : s == 5 ? rk45::CH5 : rk45::CH6;
-      qw = qmul(rot_quat(Ox, Oy, Oz, h * W), qw);
-      if (s < 6) {
-        const double E = s == 3 ? rk45::C3 : s == 4 ? rk45::C4 : rk45::C5;
-        qe = qmul(rot_quat(Ox, Oy, Oz, h * E), qe);
-      }
+      qw = qmul(rot_quat(Ox, Oy, Oz, h * cf[1]), qw);
+      if (m < 4) qe = qmul(rot_quat(Ox, Oy, Oz, h * cf[2]), qe);
     }
   }
   double cx, cy, cz;
