@@ -1,4 +1,7 @@
-// Kernels of the hot path and their launch helpers.
+// Kernels of the hot path and their launch helpers.  The window kernels
+// (k_plain, k_persistent, k_batched) are templates in st_engine.cuh; this
+// file instantiates them for integrator types 0 and 1, st_kernels_ext.cu with
+// types 2-5.
 //
 //  k_init        initParticles: seed + position + velocity + gas clock, one
 //                thread per particle (src/particle.cpp:638-710).
@@ -15,7 +18,7 @@
 //                but each lane keeps a shared-memory ring of upcoming segments,
 //                produced warp-synchronously ahead of the spin, so the step loop
 //                rarely leaves the converged path.  Template switches: the
-//                adjoint's tape, gas collisions, stage storage.
+//                adjoint's tape, gas collisions, stage storage, types 2-5.
 //  k_pack        copies the state into one snapshot block (plain path).
 #include <cuda_runtime.h>
 #include <stdint.h>
