@@ -63,6 +63,10 @@ CASES = {
                   yi="0, 1, 0", integratorType="4", rtol="1e-3", tf="0.02", ioutInt="0.005", seed="14", **G_FULL),
     "rkf45q": dict(numParticles="6", dist="C", V="5", T="0.4", gas_coll="true", diffuse="0.2", gravity="true",
                    yi="0, 0, 1", integratorType="5", rtol="1e-6", tf="0.02", ioutInt="0.005", seed="15", **G_FULL),
+    # Magnus carrying its step size across windows, gas collisions, no gravity
+    "magnus_keep": dict(numParticles="6", dist="C", V="5", T="0.4", gas_coll="true", diffuse="0.3", gravity="false",
+                        yi="1, 0, 0", integratorType="2", keepStepSize="true", tf="0.03", ioutInt="0.01", seed="21",
+                        **G_FULL),
     # RKF45's error estimate is its whole fourth-order increment: at rtol 1e-12
     # the step shrinks below hmin at once (-1)
     "rkf45_hmin": dict(numParticles="4", dist="C", V="5", gas_coll="false", diffuse="0", gravity="true",
