@@ -825,11 +825,26 @@ int st_set_params(st_ctx* c, const st_options* sets, int nsets) {
     ST_TRY(build_params(sets[k], c->sets_h[k].first, &P[k]));
   }
   ST_CUDA(cudaSetDevice(c->device));
+  // Captured run graphs hold the kernel instantiation chosen for the old sets
+  // (with or without gas collisions, integrator types 2-5) and the work order
+  // grouped by their integrators: when those change, drop both.  Values
+  // alone (fields, tolerances, times) are read from the device table.
+  bool kernels_change = false;
+  for (int k = 0; k < nsets; ++k)
+    kernels_change |= P[k].gas != c->sets_h[k].gas || P[k].integrator != c->sets_h[k].integrator;
+  if (kernels_change) {
+    ST_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+    cudaFree(c->order_d);
+    c->order_d = nullptr;
+  }
   ST_CUDA(cudaMemcpyAsync(c->sets_d, P.data(), sizeof(SetParams) * P.size(), cudaMemcpyHostToDevice, c->stream));
   if (int e = st::launch_prepare_sets(c->sets_d, nsets, c->stream))
     return fail(ST_ERR_CUDA, std::string("prepare sets: ") + cudaGetErrorString((cudaError_t)e));
   for (int k = 0; k < nsets; ++k) c->opts[k] = sets[k];
   c->sets_h = P;
+  c->adj_recorded = false;  // a recorded tape belongs to the old parameters
   return ST_OK;
 }
 

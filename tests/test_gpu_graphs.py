@@ -68,3 +68,41 @@ def test_graph_cache_follows_the_launch_configuration(gpu):
     for out in outs[1:]:
         for f in out:
             np.testing.assert_array_equal(out[f], outs[0][f], err_msg=f)
+
+
+@pytest.mark.parametrize("kernel", [st.KERNEL_PLAIN, st.KERNEL_PERSISTENT], ids=["plain", "persistent"])
+def test_set_params_keeps_or_drops_the_graphs(gpu, kernel):
+    """st_set_params with new field values keeps the captured graph (the
+    kernels read the parameter table from device memory); switching the set to
+    the Magnus stepper with gas collisions drops it (the graph holds the
+    kernel instantiation).  Either way the run equals a fresh context holding
+    the new parameters, bit for bit."""
+    base = graph_options()
+    nw = st.num_windows(base)
+    values = st.derive(st.make_options(numParticles=256, dist="M", T=4.2, diffuse=0.3, gas_coll=False, gravity=True,
+                                       Gx=(0.0, 0.0, 2e-9), E=(0.0, 0.0, -75e5), B0=(5e-6, 0.0, 0.0),
+                                       yi=(0.0, 0.0, 1.0), tf=0.2, ioutInt=0.05, seed=9))
+    kernels = st.derive(st.make_options(numParticles=256, dist="M", T=0.4, diffuse=0.3, gas_coll=True, gravity=True,
+                                        Gx=(0.0, 0.0, 1e-9), E=(0.0, 0.0, 75e5), yi=(0.0, 0.0, 1.0), tf=0.2,
+                                        ioutInt=0.05, seed=9, integratorType=2))
+
+    def fresh(opt):
+        with st.Particles(opt) as q:
+            q.init_particles()
+            q.run_windows(0, nw, kernel)
+            return q.output_data()
+
+    with st.Particles(base) as p:
+        p.init_particles()
+        p.run_windows(0, nw, kernel)
+        assert p.counters()["graph_captures"] == 1
+        for new, captures in ((values, 0), (kernels, 1)):
+            p.set_params(new)
+            p.init_particles()
+            p.run_windows(0, nw, kernel)
+            c = p.counters()
+            assert c["graph_launches"] == 1 and c["graph_captures"] == captures
+            got, ref = p.output_data(), fresh(new)
+            for f in ref:
+                np.testing.assert_array_equal(got[f], ref[f], err_msg=f)
+        assert c["ext_attempts"] > 0 and got["n_coll"].sum() > 0
