@@ -361,7 +361,7 @@ def run_workload(args):
         if args.workload == "sweep":
             sets = sweep_sets()
         elif args.workload == "dressing":
-            sets = [dressing_options(262144, 1.0)]
+            sets = [dressing_options(args.dressing_particles, args.dressing_tf)]
         else:
             sets = [_set_options(65536, 2e-9, gas_coll=True, ioutInt=2e-9)]
         psec = sum(int(o.numParticles) * st.num_windows(o) * o.ioutInt for o in sets)
@@ -657,6 +657,9 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=None,
                     help="print the line of one additional configuration instead of the headline line")
+    ap.add_argument("--dressing-particles", type=int, default=262144,
+                    help="particles of the 'dressing' workload (smaller for profiles)")
+    ap.add_argument("--dressing-tf", type=float, default=1.0, help="simulated time of the 'dressing' workload")
     ap.add_argument("--types", type=str, default="0,1,2,3,4,5",
                     help="integrator types of the 'integrators' workload (comma-separated)")
     ap.add_argument("--type-particles", type=int, default=262144,
