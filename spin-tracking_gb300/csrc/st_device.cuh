@@ -609,6 +609,47 @@ __device__ __forceinline__ void feval(const Seg& g, const SetParams& P, double t
   bloch(yx, yy, yz, Ox, Oy, Oz, fx, fy, fz);
 }
 
+// The field polynomial scaled by a step size h, so that a stage's Bloch
+// evaluation gives h k directly and its state y + sum a_j (h k_j) is an FMA
+// chain from y (ten multiplications per attempt instead of one per stage and
+// component).
+struct HPoly {
+  double o0x, o0y, o0z, o1x, o1y, o1z, o2x, o2y, o2z, gpa, h;
+};
+__device__ __forceinline__ HPoly hpoly_of(const Seg& g, double h) {
+  return {h * g.o0x, h * g.o0y, h * g.o0z, h * g.o1x, h * g.o1y, h * g.o1z,
+          h * g.o2x, h * g.o2y, h * g.o2z, h * g.gpa, h};
+}
+// h Omega at tau = t - t0 (omega_at, scaled).
+__device__ __forceinline__ void homega_at(const HPoly& q, const Seg& g, const SetParams& P, double tau, double& Ox,
+                                          double& Oy, double& Oz) {
+  Ox = fma(fma(q.o2x, tau, q.o1x), tau, q.o0x);
+  Oy = fma(fma(q.o2y, tau, q.o1y), tau, q.o0y);
+  Oz = fma(fma(q.o2z, tau, q.o1z), tau, q.o0z);
+#if !ST_GRAD_IS_LINEAR
+  {
+    const double gy = P.gravity ? 0.5 * kGravity : 0.0;
+    const Vec3 pos = {fma(g.v0x, tau, g.p0x), fma(fma(gy, tau, g.v0y), tau, g.p0y), fma(g.v0z, tau, g.p0z)};
+    const Vec3 Gp = st_grad(pos, P);
+    const double hg = q.h * P.gamma;
+    Ox = fma(hg, Gp.x, Ox);
+    Oy = fma(hg, Gp.y, Oy);
+    Oz = fma(hg, Gp.z, Oz);
+  }
+#endif
+#if ST_PULSE_IS_Z_COS
+  if (g.gpa != 0.0) Oz = fma(q.gpa, cos(P.w * (g.t0 + tau)), Oz);
+#else
+  {
+    const Vec3 pu = st_pulse(g.t0 + tau, P);
+    const double hg = q.h * P.gamma;
+    Ox = fma(hg, pu.x, Ox);
+    Oy = fma(hg, pu.y, Oy);
+    Oz = fma(hg, pu.z, Oz);
+  }
+#endif
+}
+
 // ------------------------------------------------------------ DOP853
 // Start a DOP853 call over the segment (src/integrator.cpp:102-119).
 __device__ __forceinline__ void dop_begin(Seg& g, const SetParams& P, double Sx, double Sy, double Sz, double h) {
@@ -751,37 +792,40 @@ __device__ __forceinline__ int dop_attempt_ks(Seg& g, const SetParams& P, double
   g.acc = false;
   const double tx = g.x - g.t0;
   const double S0[3] = {Sx, Sy, Sz};
-  const double k1[3] = {g.kx, g.ky, g.kz};
-  // stages 2..11: y + h * sum_j a_sj k_j, then k_s = f(x + c_s h, .)
+  // stage derivatives are carried scaled by h (ks holds h k_s)
+  const HPoly hp = hpoly_of(g, h);
+  const double k1[3] = {h * g.kx, h * g.ky, h * g.kz};
+  // stages 2..11: y + sum_j a_sj (h k_j), then h k_s = Y x (h Omega(x + c_s h))
 #pragma unroll
   for (int s = 2; s <= 11; ++s) {
     double Y[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      double acc = dopst::a(s, 0) * k1[c];
+      double acc = fma(dopst::a(s, 0), k1[c], S0[c]);
 #pragma unroll
       for (int j = 1; j < dopst::cnt(s); ++j) acc = fma(dopst::a(s, j), ks.k(dopst::src(s, j), c), acc);
-      Y[c] = fma(h, acc, S0[c]);
+      Y[c] = acc;
     }
-    double kx, ky, kz;
-    feval(g, P, fma(dopst::c(s), h, tx), Y[0], Y[1], Y[2], kx, ky, kz);
+    double Ox, Oy, Oz, kx, ky, kz;
+    homega_at(hp, g, P, fma(dopst::c(s), h, tx), Ox, Oy, Oz);
+    bloch(Y[0], Y[1], Y[2], Ox, Oy, Oz, kx, ky, kz);
     ks.k(s, 0) = kx;
     ks.k(s, 1) = ky;
     ks.k(s, 2) = kz;
   }
-  // stage 12 at x + h; its Omega is reused for the FSAL derivative
+  // stage 12 at x + h; its unscaled Omega is reused for the FSAL derivative
   double Y12[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    double acc = dopst::a(12, 0) * k1[c];
+    double acc = fma(dopst::a(12, 0), k1[c], S0[c]);
 #pragma unroll
     for (int j = 1; j < dopst::cnt(12); ++j) acc = fma(dopst::a(12, j), ks.k(dopst::src(12, j), c), acc);
-    Y12[c] = fma(h, acc, S0[c]);
+    Y12[c] = acc;
   }
   const double tph = tx + h;
   double Ox12, Oy12, Oz12, k12[3];
   omega_at(g, P, tph, Ox12, Oy12, Oz12);
-  bloch(Y12[0], Y12[1], Y12[2], Ox12, Oy12, Oz12, k12[0], k12[1], k12[2]);
+  bloch(Y12[0], Y12[1], Y12[2], h * Ox12, h * Oy12, h * Oz12, k12[0], k12[1], k12[2]);
   // 8th-order combination and the new state
   double bsum[3];
 #pragma unroll
@@ -796,8 +840,9 @@ __device__ __forceinline__ int dop_attempt_ks(Seg& g, const SetParams& P, double
     bsum[c] = fma(B12, k12[c], acc);
   }
   const double bx = bsum[0], by = bsum[1], bz = bsum[2];
-  const double nx = fma(h, bx, Sx), ny = fma(h, by, Sy), nz = fma(h, bz, Sz);
-  // error estimates: 3rd-order (bhh) and 5th-order (er) rows
+  const double nx = Sx + bx, ny = Sy + by, nz = Sz + bz;
+  // error estimates: 3rd-order (bhh) and 5th-order (er) rows, h times the
+  // reference's; the scale cancels in err = |h| err_5 / sqrt(3 (err_5 + 0.01 err_3))
   const double e1x = fma(-BHH3, k12[0], fma(-BHH2, ks.k(9, 0), fma(-BHH1, k1[0], bx)));
   const double e1y = fma(-BHH3, k12[1], fma(-BHH2, ks.k(9, 1), fma(-BHH1, k1[1], by)));
   const double e1z = fma(-BHH3, k12[2], fma(-BHH2, ks.k(9, 2), fma(-BHH1, k1[2], bz)));
@@ -823,7 +868,7 @@ __device__ __forceinline__ int dop_attempt_ks(Seg& g, const SetParams& P, double
   double err = fma(q2z, q2z, fma(q2y, q2y, q2x * q2x));
   double deno = fma(0.01, err2, err);
   if (deno <= 0.0) deno = 1.0;
-  err = (fabs(h) * err) * rsqrt_full(deno * 3.0);
+  err = err * rsqrt_full(deno * 3.0);
   // step-size controller (Lund-stabilised, clamped to [1/fac2, 1/fac1])
   double hnew;
   const bool fast = (P.beta == 0.0) && (err > 1e-300) && (err < 1e300);
