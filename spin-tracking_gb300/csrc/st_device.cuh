@@ -956,35 +956,44 @@ __device__ __forceinline__ int rk45_attempt(Seg& g, const SetParams& P, double& 
     stop = false;
   }
   const double tx = g.x - g.t0;
+  // stage derivatives scaled by h (k below is h f), as in the DOP853 attempt
+  const HPoly hp = hpoly_of(g, h);
   double k1x, k1y, k1z, k2x, k2y, k2z, k3x, k3y, k3z, k4x, k4y, k4z, k5x, k5y, k5z, k6x, k6y, k6z;
-  double yx, yy, yz;
-  feval(g, P, tx, g.kx, g.ky, g.kz, k1x, k1y, k1z);
-  yx = fma(h * B21, k1x, Sx); yy = fma(h * B21, k1y, Sy); yz = fma(h * B21, k1z, Sz);
-  feval(g, P, fma(A2, h, tx), yx, yy, yz, k2x, k2y, k2z);
-  yx = fma(h, fma(B32, k2x, B31 * k1x), Sx);
-  yy = fma(h, fma(B32, k2y, B31 * k1y), Sy);
-  yz = fma(h, fma(B32, k2z, B31 * k1z), Sz);
-  feval(g, P, fma(A3, h, tx), yx, yy, yz, k3x, k3y, k3z);
-  yx = fma(h, fma(B43, k3x, fma(B42, k2x, B41 * k1x)), Sx);
-  yy = fma(h, fma(B43, k3y, fma(B42, k2y, B41 * k1y)), Sy);
-  yz = fma(h, fma(B43, k3z, fma(B42, k2z, B41 * k1z)), Sz);
-  feval(g, P, fma(A4, h, tx), yx, yy, yz, k4x, k4y, k4z);
-  yx = fma(h, fma(B54, k4x, fma(B53, k3x, fma(B52, k2x, B51 * k1x))), Sx);
-  yy = fma(h, fma(B54, k4y, fma(B53, k3y, fma(B52, k2y, B51 * k1y))), Sy);
-  yz = fma(h, fma(B54, k4z, fma(B53, k3z, fma(B52, k2z, B51 * k1z))), Sz);
-  feval(g, P, fma(A5, h, tx), yx, yy, yz, k5x, k5y, k5z);
-  yx = fma(h, fma(B65, k5x, fma(B64, k4x, fma(B63, k3x, fma(B62, k2x, B61 * k1x)))), Sx);
-  yy = fma(h, fma(B65, k5y, fma(B64, k4y, fma(B63, k3y, fma(B62, k2y, B61 * k1y)))), Sy);
-  yz = fma(h, fma(B65, k5z, fma(B64, k4z, fma(B63, k3z, fma(B62, k2z, B61 * k1z)))), Sz);
-  feval(g, P, fma(A6, h, tx), yx, yy, yz, k6x, k6y, k6z);
+  double yx, yy, yz, Ox, Oy, Oz;
+  homega_at(hp, g, P, tx, Ox, Oy, Oz);
+  bloch(g.kx, g.ky, g.kz, Ox, Oy, Oz, k1x, k1y, k1z);
+  yx = fma(B21, k1x, Sx); yy = fma(B21, k1y, Sy); yz = fma(B21, k1z, Sz);
+  homega_at(hp, g, P, fma(A2, h, tx), Ox, Oy, Oz);
+  bloch(yx, yy, yz, Ox, Oy, Oz, k2x, k2y, k2z);
+  yx = fma(B32, k2x, fma(B31, k1x, Sx));
+  yy = fma(B32, k2y, fma(B31, k1y, Sy));
+  yz = fma(B32, k2z, fma(B31, k1z, Sz));
+  homega_at(hp, g, P, fma(A3, h, tx), Ox, Oy, Oz);
+  bloch(yx, yy, yz, Ox, Oy, Oz, k3x, k3y, k3z);
+  yx = fma(B43, k3x, fma(B42, k2x, fma(B41, k1x, Sx)));
+  yy = fma(B43, k3y, fma(B42, k2y, fma(B41, k1y, Sy)));
+  yz = fma(B43, k3z, fma(B42, k2z, fma(B41, k1z, Sz)));
+  homega_at(hp, g, P, fma(A4, h, tx), Ox, Oy, Oz);
+  bloch(yx, yy, yz, Ox, Oy, Oz, k4x, k4y, k4z);
+  yx = fma(B54, k4x, fma(B53, k3x, fma(B52, k2x, fma(B51, k1x, Sx))));
+  yy = fma(B54, k4y, fma(B53, k3y, fma(B52, k2y, fma(B51, k1y, Sy))));
+  yz = fma(B54, k4z, fma(B53, k3z, fma(B52, k2z, fma(B51, k1z, Sz))));
+  homega_at(hp, g, P, fma(A5, h, tx), Ox, Oy, Oz);
+  bloch(yx, yy, yz, Ox, Oy, Oz, k5x, k5y, k5z);
+  yx = fma(B65, k5x, fma(B64, k4x, fma(B63, k3x, fma(B62, k2x, fma(B61, k1x, Sx)))));
+  yy = fma(B65, k5y, fma(B64, k4y, fma(B63, k3y, fma(B62, k2y, fma(B61, k1y, Sy)))));
+  yz = fma(B65, k5z, fma(B64, k4z, fma(B63, k3z, fma(B62, k2z, fma(B61, k1z, Sz)))));
+  homega_at(hp, g, P, fma(A6, h, tx), Ox, Oy, Oz);
+  bloch(yx, yy, yz, Ox, Oy, Oz, k6x, k6y, k6z);
   g.kx = yx; g.ky = yy; g.kz = yz;  // the next attempt's first stage sees this state
-  // CH2 and CT2 are zero: k2 does not enter the weights
+  // CH2 and CT2 are zero: k2 does not enter the weights; the new state adds
+  // the small weighted sum to S in one rounding
   const double wx = fma(CH6, k6x, fma(CH5, k5x, fma(CH4, k4x, fma(CH3, k3x, CH1 * k1x))));
   const double wy = fma(CH6, k6y, fma(CH5, k5y, fma(CH4, k4y, fma(CH3, k3y, CH1 * k1y))));
   const double wz = fma(CH6, k6z, fma(CH5, k5z, fma(CH4, k4z, fma(CH3, k3z, CH1 * k1z))));
-  const double tex = h * fma(CT6, k6x, fma(CT5, k5x, fma(CT4, k4x, fma(CT3, k3x, CT1 * k1x))));
-  const double tey = h * fma(CT6, k6y, fma(CT5, k5y, fma(CT4, k4y, fma(CT3, k3y, CT1 * k1y))));
-  const double tez = h * fma(CT6, k6z, fma(CT5, k5z, fma(CT4, k4z, fma(CT3, k3z, CT1 * k1z))));
+  const double tex = fma(CT6, k6x, fma(CT5, k5x, fma(CT4, k4x, fma(CT3, k3x, CT1 * k1x))));
+  const double tey = fma(CT6, k6y, fma(CT5, k5y, fma(CT4, k4y, fma(CT3, k3y, CT1 * k1y))));
+  const double tez = fma(CT6, k6z, fma(CT5, k5z, fma(CT4, k4z, fma(CT3, k3z, CT1 * k1z))));
   double error = sqrt(fma(tez, tez, fma(tey, tey, tex * tex)));
   error = std_max(error, 1.0e-16);
   const double ratio = P.rtol / error;
@@ -992,9 +1001,9 @@ __device__ __forceinline__ int rk45_attempt(Seg& g, const SetParams& P, double& 
   double q = exp(E1 * lnr + E2 * g.lnprev);  // ratio^E1 * prev_ratio^E2
   q = std_min(q, 4.0);
   if ((q > 0.81 && error < 2.0 * P.rtol) || P.fixed) {
-    const double ny = fma(h, wy, Sy), nz = fma(h, wz, Sz);
+    const double ny = Sy + wy, nz = Sz + wz;
     g.turns += count_turn(Sy, Sz, ny, nz);
-    Sx = fma(h, wx, Sx); Sy = ny; Sz = nz;
+    Sx = Sx + wx; Sy = ny; Sz = nz;
     g.x += h;
     if (stop) {
       g.h = g.lastH;
