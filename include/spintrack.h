@@ -294,7 +294,9 @@ int st_probe_fp64_peak(int device, double *tflops);
 /* Derive tc/sqrtKT_m, create, init, write the options header and the t0
  * snapshot, run every window with `kernel`, append a snapshot per window
  * (format 'A', src/logger.cpp:14-38).  run_seconds (may be NULL) receives the
- * wall time of the window loop excluding file writes. */
+ * wall time of the window loop excluding file writes.  A path ending in .h5 or
+ * .hdf5 (any case) is refused with ST_ERR_UNSUPPORTED, as by a reference
+ * build without HDF5 (createLogger, src/logger.cpp:192-204). */
 int st_main_analysis(const st_options *opt, const char *out_path, int device, int kernel, double *run_seconds);
 /* Format 'A' writer pieces, for callers that hold their own state. */
 int st_write_header(void *file /* FILE* */, const st_options *opt);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <cerrno>
 #include <chrono>
 #include <cmath>
@@ -1430,6 +1431,16 @@ void unpack_block(const st_ctx* c, const char* blk, HostSnap& hs) {
 extern "C" int st_main_analysis(const st_options* opt_in, const char* out_path, int device, int kernel,
                                 double* run_seconds) {
   if (!opt_in || !out_path) return fail(ST_ERR_ARG, "null argument");
+  {
+    // createLogger (src/logger.cpp:192-204) picks HDF5 by the file extension;
+    // like a reference build without HDF5, refuse such a name before any work
+    std::string ext = out_path;
+    const size_t dot = ext.find_last_of('.'), slash = ext.find_last_of('/');
+    ext = (dot == std::string::npos || (slash != std::string::npos && dot < slash)) ? "" : ext.substr(dot);
+    for (auto& ch : ext) ch = (char)std::tolower(static_cast<unsigned char>(ch));
+    if (ext == ".hdf5" || ext == ".h5")
+      return fail(ST_ERR_UNSUPPORTED, "HDF5 output is not built, but the output file has an hdf5 extension");
+  }
   st_options opt = *opt_in;
   st_derive(&opt);
   st_ctx* c = nullptr;

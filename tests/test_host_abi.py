@@ -139,3 +139,15 @@ def test_create_rejects_before_device_work(stlib, field, value, code):
     assert stlib.st_create(ctypes.byref(o), 0, ctypes.byref(ctx)) == code
     assert not ctx.value
     assert stlib.st_last_error()
+
+
+@pytest.mark.parametrize("name", ["out.h5", "OUT.HDF5", "run.Hdf5"])
+def test_main_analysis_refuses_hdf5_names_before_device_work(stlib, tmp_path, name):
+    """createLogger picks HDF5 by extension; a reference build without HDF5
+    throws for such a name, and so does st_main_analysis (before any GPU call)."""
+    o = Options()
+    stlib.st_options_default(ctypes.byref(o))
+    path = tmp_path / name
+    assert stlib.st_main_analysis(ctypes.byref(o), str(path).encode(), 0, 1, None) == _capi.ST_ERR_UNSUPPORTED
+    assert b"HDF5" in stlib.st_last_error()
+    assert not path.exists()
