@@ -199,7 +199,7 @@ int st_get_counters(const st_ctx *ctx, st_counters *out);
  * `stream` (a cudaStream_t, NULL = default stream) before returning. */
 int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state_bytes, int w_end, void *stream);
 
-/* ---- discrete adjoint (DOP853, fixed accepted-step sequence) ----------- */
+/* ---- discrete adjoint (DOP853 or Magnus CFET8, fixed accepted steps) --- */
 /* Gradient parameters, in this order: the gradient tensor rows Gx, Gy, Gz
  * (9: B_i = dot(pos, G_i)), B0 (3), E (3), pulse amplitude a and angular
  * frequency w (2). */
@@ -207,14 +207,16 @@ int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state
 /* Forward pass for st_adjoint_backward, from a freshly initialised context
  * (st_init): advances every particle through windows [0, w_end) exactly as
  * st_run_windows does (the trajectory-ahead kernel), and writes the adjoint's
- * tape: every accepted DOP853 step (y, x, h) and every integrated segment
+ * tape: every accepted step (y, x, h) and every integrated segment
  * (t0, p0, v0) of every particle, in pages of a device pool of tape_bytes
  * (0 = up to 45% of free device memory).  It also keeps a full-state
  * checkpoint every windows_per_checkpoint windows (0 = chosen so the
  * checkpoints take at most 10% of free memory).  When the tape does not fit
  * the pool, st_adjoint_backward replays window chunks from the checkpoints
  * (and, if one window's tape does not fit, groups of particles), so results
- * do not depend on the pool size.  DOP853 sets and the linear grad hook only.
+ * do not depend on the pool size.  All sets of the context integrate with
+ * DOP853 (integratorType 0) or all with Magnus CFET8 (2); the linear grad
+ * hook only.
  * No counterpart in the reference (it has no derivatives). */
 int st_adjoint_record(st_ctx *ctx, int w_end, size_t tape_bytes, int windows_per_checkpoint);
 /* Backward pass: given dL/dS_final for every particle (device array,

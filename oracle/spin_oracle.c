@@ -33,7 +33,7 @@ static or_counters *g_counters = NULL;
 void or_set_counters(or_counters *c) { g_counters = c; }
 
 /* Frozen accepted-step log (finite-difference checks of the adjoint): mode 1
- * appends every accepted DOP853 step (h, last) to the log; mode 2 replays the
+ * appends every accepted step (h, last) of DOP853 and of integrator types 2-5 to the log; mode 2 replays the
  * log instead of the step controller (every step accepted with the logged h).
  * Runs that use the log must be single-threaded. */
 static double *g_log = NULL;
@@ -749,7 +749,15 @@ int or_integrate_ext(const or_options *o, double t0, double tf, or_vec3 *yio, co
     }
     double endDt = tf - t;
     lastH = h;
-    if (o->fixedStepSize) {
+    if (g_log_mode == 2) { /* replay: the logged accepted step */
+      if (g_log_n >= g_log_cap) {
+        *yio = y;
+        return -9;
+      }
+      h = g_log[2 * g_log_n];
+      stop = g_log[2 * g_log_n + 1] != 0.0;
+      g_log_n++;
+    } else if (o->fixedStepSize) {
       h = o->h;
     } else if (h >= endDt) {
       h = endDt;
@@ -772,7 +780,12 @@ int or_integrate_ext(const or_options *o, double t0, double tf, or_vec3 *yio, co
     double ratio = tol / error;
     double q = pow(ratio, e1) * pow(prev_ratio, e2);
     q = std_min(q, 4.0);
-    if ((q > 0.81 && error < 2 * tol) || o->fixedStepSize) {
+    if ((q > 0.81 && error < 2 * tol) || o->fixedStepSize || g_log_mode == 2) {
+      if (g_log_mode == 1 && g_log_n < g_log_cap) {
+        g_log[2 * g_log_n] = h;
+        g_log[2 * g_log_n + 1] = stop ? 1.0 : 0.0;
+        g_log_n++;
+      }
       y = ws;
       t += h;
       if (stop) {

@@ -110,7 +110,7 @@ typedef struct { uint64_t dop_attempts, rk45_attempts, segments, ext_attempts; }
 void or_set_counters(or_counters *c);
 
 /* Frozen accepted-step log for finite-difference checks: mode 1 records every
- * accepted DOP853 step as (h, last), mode 2 replays the record in place of the
+ * accepted DOP853 / type 2-5 step as (h, last), mode 2 replays the record in place of the
  * step controller, 0 = off.  Single-threaded runs only. */
 void or_set_step_log(double *buf, int64_t cap, int mode);
 int64_t or_step_log_count(void);

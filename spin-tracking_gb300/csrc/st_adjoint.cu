@@ -1,6 +1,6 @@
-// Discrete adjoint of the DOP853 spin integration along the particles' fixed
-// trajectories: gradients of a loss L(S_final) with respect to the field
-// parameters theta = [Gx(3), Gy(3), Gz(3), B0(3), E(3), a, w].
+// Discrete adjoint of the DOP853 (and Magnus CFET8) spin integration along the
+// particles' fixed trajectories: gradients of a loss L(S_final) with respect
+// to the field parameters theta = [Gx(3), Gy(3), Gz(3), B0(3), E(3), a, w].
 //
 // The trajectory does not depend on theta, and with the accepted step
 // sequence held fixed every DOP853 step is a linear map of the spin, so the
@@ -122,6 +122,118 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
 #undef ST_OS
 }
 
+// Rodrigues rotation v' = R(k) v = v cos a + (v x k) sin(a)/a + k (k.v)(1 - cos a)/a^2
+// (a = |k|, rodrigues in st_device.cuh): given mu = dL/dv', return dL/dk in gk
+// and replace mu by dL/dv = R(k)^T mu = R(-k) mu.  With al = cos a,
+// be = sin(a)/a, ga = (1 - cos a)/a^2 and their a-derivatives,
+//   dL/dk = k/a (al' v.mu + be' (v x k).mu + ga' (k.v)(k.mu)) + be (mu x v)
+//           + ga ((k.mu) v + (k.v) mu).
+__device__ __forceinline__ void rodrigues_adjoint(const double k[3], const double v[3], double mu[3], double gk[3]) {
+  const double a2 = fma(k[2], k[2], fma(k[1], k[1], k[0] * k[0]));
+  const double r = rsqrt(a2);
+  const double a = a2 * r;
+  double s, c;
+  sincos(a, &s, &c);
+  const double omc = 1.0 - c;
+  const double be = s * r, ga = omc * (r * r);
+  const double dal = -s;
+  const double dbe = (a * c - s) * (r * r);
+  const double dga = (a * s - 2.0 * omc) * (r * r * r);
+  const double vm = v[0] * mu[0] + v[1] * mu[1] + v[2] * mu[2];
+  const double kv = k[0] * v[0] + k[1] * v[1] + k[2] * v[2];
+  const double km = k[0] * mu[0] + k[1] * mu[1] + k[2] * mu[2];
+  double vk[3], mv[3], mk[3];
+  cross3(v, k, vk);
+  cross3(mu, v, mv);
+  cross3(mu, k, mk);
+  const double vkm = vk[0] * mu[0] + vk[1] * mu[1] + vk[2] * mu[2];
+  const double coef = (dal * vm + dbe * vkm + dga * kv * km) * r;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) gk[q] = fma(coef, k[q], fma(be, mv[q], ga * fma(km, v[q], kv * mu[q])));
+  // R(-k) mu = mu cos a - (mu x k) sin(a)/a + k (k.mu)(1 - cos a)/a^2
+  const double d = km * ga;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) mu[q] = fma(k[q], d, fma(-be, mk[q], mu[q] * c));
+}
+
+// Backward through one accepted Magnus CFET8 step from (x, y) with step h
+// (magnus_stages in st_device.cuh; the CFET6 companion only estimated the
+// error and does not enter the accepted map): the field at the five
+// Gauss-Legendre nodes is recomputed, the 11 rotations are replayed with
+// their inputs kept in shared memory (sm[(n * 3 + c) * BLOCK]), then undone
+// last first, each giving dL/dk_n; dL/d(h Omega_j) = sum_n G_nj dL/dk_n and
+// z_j = h dL/d(h Omega_j) is dL/dOmega at node j, accumulated into the
+// segment moments like the DOP853 stages.
+template <int BLOCK>
+__device__ __forceinline__ void magnus_step_adjoint(const Seg& g, const SetParams& P, double x, double h,
+                                                    const double y[3], double lam[3], Moments& M, bool pulse,
+                                                    double* sm) {
+#define ST_VN(n, c) sm[((n) * 3 + (c)) * BLOCK]
+  const double tx = x - g.t0;
+  double B[5][3];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    omega_at(g, P, fma(cfetc::x(i), h, tx), B[i][0], B[i][1], B[i][2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B[i][c] *= h;
+  }
+  double v[3] = {y[0], y[1], y[2]};
+#pragma unroll 1
+  for (int n = 0; n < 11; ++n) {
+    const double* cf = kMagnusExp[n];
+    double k[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double s = cf[0] * B[0][c];
+#pragma unroll
+      for (int j = 1; j < 5; ++j) s = fma(cf[j], B[j][c], s);
+      k[c] = s;
+      ST_VN(n, c) = v[c];
+    }
+    rodrigues(k[0], k[1], k[2], v[0], v[1], v[2]);
+  }
+  double zb[5][3] = {};  // dL/d(h Omega_j)
+#pragma unroll 1
+  for (int n = 10; n >= 0; --n) {
+    const double* cf = kMagnusExp[n];
+    double k[3], vn[3], gk[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double s = cf[0] * B[0][c];
+#pragma unroll
+      for (int j = 1; j < 5; ++j) s = fma(cf[j], B[j][c], s);
+      k[c] = s;
+      vn[c] = ST_VN(n, c);
+    }
+    rodrigues_adjoint(k, vn, lam, gk);
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) zb[j][c] = fma(cf[j], gk[c], zb[j][c]);
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const double tau = fma(cfetc::x(j), h, tx);
+    const double tau2 = tau * tau;
+    double z[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      z[c] = h * zb[j][c];
+      M.z0[c] += z[c];
+      M.z1[c] = fma(z[c], tau, M.z1[c]);
+      M.z2[c] = fma(z[c], tau2, M.z2[c]);
+    }
+    if (pulse) {
+      const double t = g.t0 + tau;
+      double sn, cs;
+      sincos(P.w * t, &sn, &cs);
+      M.ga = fma(P.gamma * cs, z[2], M.ga);
+      M.gw = fma(-P.gamma * P.a * t * sn, z[2], M.gw);
+    }
+  }
+#undef ST_VN
+}
+
 // Contract a segment's moments into dL/dtheta (theta order of the file header);
 // gth is strided by `stride` (shared memory, one column per thread).
 __device__ __forceinline__ void contract(const SetParams& P, const double p0[3], const double v0[3], const Moments& M,
@@ -177,6 +289,8 @@ __device__ __forceinline__ void tape_load_seg(const TapeArgs& t, const SetParams
 // exhausted.  Reads lam and adds to grad per particle; the tape's
 // consistency (both chains end together, page indices inside the pool) is
 // checked and a violation sets t.error and abandons the particle.
+// MAGNUS: the tape holds Magnus CFET8 steps (integratorType 2) instead of DOP853 ones.
+template <bool MAGNUS>
 __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs t) {
   __shared__ double stage_all[2 * 12 * 3 * kAdjBlock];  // stage states, then stage fields
   __shared__ double gsm_all[kNumTheta * kAdjBlock];
@@ -236,7 +350,10 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
     const double y[3] = {r[0], r[1], r[2]};
     const double x = r[3], h = r[4];
     const bool first = x == g.t0;  // the segment's first step starts at its t0
-    dop_step_adjoint<kAdjBlock>(g, *P, x, h, y, lam, M, pulse, stg);
+    if (MAGNUS)
+      magnus_step_adjoint<kAdjBlock>(g, *P, x, h, y, lam, M, pulse, stg);
+    else
+      dop_step_adjoint<kAdjBlock>(g, *P, x, h, y, lam, M, pulse, stg);
     ++walked_s;
     bool finish = false;
     int bad = 0;
@@ -296,15 +413,21 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
 // ---------------------------------------------------------------- launchers
 int adj_backward_block() { return kAdjBlock; }
 
-int adj_backward_max_blocks_per_sm() {
+int adj_backward_max_blocks_per_sm(int magnus) {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_adj_backward, kAdjBlock, 0);
+  if (magnus)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_adj_backward<true>, kAdjBlock, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_adj_backward<false>, kAdjBlock, 0);
   return nb;
 }
 
-int launch_adj_backward(const RunArgs& a, const TapeArgs& t, int blocks, void* stream) {
+int launch_adj_backward(const RunArgs& a, const TapeArgs& t, int blocks, int magnus, void* stream) {
   if (a.nitems == 0) return 0;
-  k_adj_backward<<<blocks, kAdjBlock, 0, (cudaStream_t)stream>>>(a, t);
+  if (magnus)
+    k_adj_backward<true><<<blocks, kAdjBlock, 0, (cudaStream_t)stream>>>(a, t);
+  else
+    k_adj_backward<false><<<blocks, kAdjBlock, 0, (cudaStream_t)stream>>>(a, t);
   return (int)cudaGetLastError();
 }
 

@@ -952,7 +952,7 @@ int adj_reset_tape(st_ctx* c) {
 }
 
 int adj_tape_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) {
-  const int per_sm = std::max(1, st::tape_record_max_blocks_per_sm());
+  const int per_sm = std::max(1, st::tape_record_max_blocks_per_sm(ctx_any_ext(c) ? 1 : 0));
   int e = st::launch_tape_record(a, t, c->sm_count * per_sm, c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("adjoint tape launch: ") + cudaGetErrorString((cudaError_t)e));
   return ST_OK;
@@ -960,8 +960,9 @@ int adj_tape_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) {
 
 int adj_backward_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) {
   ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
-  const int per_sm = std::max(1, st::adj_backward_max_blocks_per_sm());
-  int e = st::launch_adj_backward(a, t, c->sm_count * per_sm, c->stream);
+  const int magnus = ctx_any_ext(c) ? 1 : 0;  // the record pass admits types 0 or 2, one per context
+  const int per_sm = std::max(1, st::adj_backward_max_blocks_per_sm(magnus));
+  int e = st::launch_adj_backward(a, t, c->sm_count * per_sm, magnus, c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("adjoint backward launch: ") + cudaGetErrorString((cudaError_t)e));
   long long rep[st::kTapeErrorSlots] = {};
   ST_CUDA(cudaMemcpyAsync(rep, c->tape_error, sizeof(rep), cudaMemcpyDeviceToHost, c->stream));
@@ -1122,7 +1123,9 @@ int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_c
 #endif
   int nwin_max = 0;
   for (const auto& P : c->sets_h) {
-    if (P.integrator != 0) return fail(ST_ERR_UNSUPPORTED, "the adjoint differentiates DOP853 (integratorType 0) only");
+    if (P.integrator != c->sets_h[0].integrator || (P.integrator != 0 && P.integrator != 2))
+      return fail(ST_ERR_UNSUPPORTED,
+                  "the adjoint differentiates DOP853 or Magnus CFET8 (integratorType 0 or 2), one type per context");
     nwin_max = std::max(nwin_max, P.nwin);
   }
   ST_CUDA(cudaSetDevice(c->device));

@@ -1257,6 +1257,7 @@ __device__ __forceinline__ void ext_begin(Seg& g, double h) { rk45_begin(g, h); 
 __device__ __forceinline__ int ext_attempt(Seg& g, const SetParams& P, double& Sx, double& Sy, double& Sz) {
   g.nstep++;
   if (g.nstep > P.nmax) return -2;
+  g.acc = false;
   const double endDt = g.xf - g.x;
   double h = g.h;
   g.lastH = h;
@@ -1288,6 +1289,8 @@ __device__ __forceinline__ int ext_attempt(Seg& g, const SetParams& P, double& S
   double q = exp(rk45::E1 * lnr + rk45::E2 * g.lnprev);  // ratio^E1 * prev_ratio^E2
   q = std_min(q, 4.0);
   if ((q > 0.81 && error < 2.0 * P.rtol) || P.fixed) {
+    g.acc = true;  // read by the adjoint's tape writer
+    g.hu = h;
     g.turns += count_turn(Sy, Sz, w[1], w[2]);
     Sx = w[0]; Sy = w[1]; Sz = w[2];
     g.x += h;

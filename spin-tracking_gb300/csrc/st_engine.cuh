@@ -405,7 +405,7 @@ __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, d
     r[11 * BLOCK] = s0.vx; r[12 * BLOCK] = s0.vy; r[13 * BLOCK] = s0.vz;
 #endif
   }
-  // the segments the spin side integrates, in order (the tape is DOP853-only)
+  // the segments the spin side integrates, in order
   if (TAPE && !tp.stop && tp.fail == 0) tape_seg(ta, tc, s0);
   qf[slot * BLOCK + tid] = (fin ? 1 : 0) | (tp.stop ? 2 : 0) | (tp.n_bounce != nb ? 4 : 0) |
                            (tp.n_coll != nc ? 8 : 0) | ((tp.fail & 0xff) << 8);
@@ -610,8 +610,10 @@ __global__ void __launch_bounds__(BLOCK, MINB)
         r = rk45_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
         ++n_rk;
       } else {
+        const double y0x = tp.Sx, y0y = tp.Sy, y0z = tp.Sz, x0 = g.x;
         r = ext_attempt(g, *P, tp.Sx, tp.Sy, tp.Sz);
         ++n_ext;
+        if (TAPE && g.acc) tape_step(ta, tc, y0x, y0y, y0z, x0, g.hu);
       }
       if (r != 0) {
         tempH = g.h;
@@ -643,9 +645,15 @@ __global__ void __launch_bounds__(BLOCK, MINB)
 }
 
 // ------------------------------------------------------------------ EXT instantiations
+// The adjoint's record pass: the trajectory-ahead kernel with its tape on, in
+// one configuration.
+constexpr int kTapeBlock = 128, kTapeQcap = 6;
+
 // Defined in st_kernels_ext.cu: the kernel of persistent variant v with
-// integrator types 2-5, and the plain kernel's launch with them.
+// integrator types 2-5, the record pass with them (gas-capable), and the plain
+// kernel's launch with them.
 const void* variant_fn_ext(int v);
+const void* tape_fn_ext();
 int launch_plain_ext(const RunArgs& a, int window, double next_t, int block, void* stream);
 
 }  // namespace st

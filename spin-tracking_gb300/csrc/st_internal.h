@@ -145,12 +145,12 @@ struct TapeArgs {
   long long* error;               // kTapeErrorSlots: first inconsistency found (code, particle, cursors)
 };
 // The trajectory-ahead kernel with its tape switch on (st_kernels.cu).
-int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);
+int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);  // a.any_ext: Magnus
 int tape_record_block();
-int tape_record_max_blocks_per_sm();
-int launch_adj_backward(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);
+int tape_record_max_blocks_per_sm(int ext);
+int launch_adj_backward(const RunArgs& a, const TapeArgs& t, int blocks, int magnus, void* stream);
 int adj_backward_block();
-int adj_backward_max_blocks_per_sm();
+int adj_backward_max_blocks_per_sm(int magnus);
 
 // Ensemble statistics (st_ensemble.cu).
 int ensemble_device(const double* t, const double* Sx, const double* Sy, const double* Sz, const int32_t* fail,

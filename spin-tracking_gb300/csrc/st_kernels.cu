@@ -266,41 +266,44 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
 }
 
 // The record pass of the adjoint: the trajectory-ahead kernel with its tape on
-// (one configuration: 128 lanes, 6-record rings, top-up at 24 / 16 lanes).
-constexpr int kTapeBlock = 128, kTapeQcap = 6;
-static const void* tape_fn(bool gas) {
+// (one configuration: kTapeBlock lanes, kTapeQcap-record rings, top-up at 24 /
+// 16 lanes); the EXT instantiation (st_kernels_ext.cu) records Magnus steps.
+static const void* tape_fn(bool gas, bool ext) {
+  if (ext) return tape_fn_ext();
   return gas ? reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, true, 0, false>)
              : reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, false, 0, false>);
 }
 static size_t tape_smem() { return batched_smem(kTapeBlock, kTapeQcap, 0); }
 
-static cudaError_t tape_ensure_smem(bool gas) {
-  static bool done[2] = {};
-  if (done[gas]) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(tape_fn(gas), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tape_smem());
-  if (e == cudaSuccess) done[gas] = true;
+static cudaError_t tape_ensure_smem(bool gas, bool ext) {
+  static bool done[3] = {};
+  const int k = ext ? 2 : (gas ? 1 : 0);
+  if (done[k]) return cudaSuccess;
+  cudaError_t e =
+      cudaFuncSetAttribute(tape_fn(gas, ext), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tape_smem());
+  if (e == cudaSuccess) done[k] = true;
   return e;
 }
 
 int tape_record_block() { return kTapeBlock; }
 
-int tape_record_max_blocks_per_sm() {
+int tape_record_max_blocks_per_sm(int ext) {
   int nb = 0;
-  if (tape_ensure_smem(true) != cudaSuccess) return 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tape_fn(true), kTapeBlock, tape_smem());
+  if (tape_ensure_smem(true, ext != 0) != cudaSuccess) return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tape_fn(true, ext != 0), kTapeBlock, tape_smem());
   return nb;
 }
 
 int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream) {
   if (a.nitems == 0) return 0;
-  const bool gas = a.any_gas != 0;
-  cudaError_t e = tape_ensure_smem(gas);
+  const bool gas = a.any_gas != 0, ext = a.any_ext != 0;
+  cudaError_t e = tape_ensure_smem(gas, ext);
   if (e != cudaSuccess) return (int)e;
   RunArgs args = a;
   TapeArgs tape = t;
   int t0 = 24, t1 = 16, dk = 12;
   void* params[] = {&args, &t0, &t1, &dk, &tape};
-  return (int)cudaLaunchKernel(tape_fn(gas), dim3(blocks), dim3(kTapeBlock), params, tape_smem(),
+  return (int)cudaLaunchKernel(tape_fn(gas, ext), dim3(blocks), dim3(kTapeBlock), params, tape_smem(),
                                (cudaStream_t)stream);
 }
 

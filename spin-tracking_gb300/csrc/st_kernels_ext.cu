@@ -25,6 +25,10 @@ const void* variant_fn_ext(int v) {
   }
 }
 
+const void* tape_fn_ext() {
+  return reinterpret_cast<const void*>(&k_batched<kTapeBlock, 1, kTapeQcap, true, true, 0, true>);
+}
+
 template <int B>
 static int plain_launch_ext(const RunArgs& a, int window, double next_t, void* stream) {
   k_plain<B, true><<<(unsigned)((a.s.n + B - 1) / B), B, 0, (cudaStream_t)stream>>>(a, window, next_t);

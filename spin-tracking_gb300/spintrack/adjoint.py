@@ -7,8 +7,9 @@ theta has one row per parameter set, ST_NUM_THETA = 17 columns:
     E(3)                 electric field, V/m
     a, w                 pulse amplitude (T) and angular frequency (rad/s)
 The forward returns the final spins (N x 3, float64, on the engine's device);
-gradients are exact for the accepted DOP853 step sequence of that forward
-pass (the adaptive step choice is held fixed).
+gradients are exact for the accepted step sequence of that forward pass (the
+adaptive step choice is held fixed), with the DOP853 or the Magnus CFET8
+stepper (integratorType 0 or 2, one per engine).
 """
 from __future__ import annotations
 

@@ -1,9 +1,10 @@
-"""The discrete adjoint against finite differences.
+"""The discrete adjoint against finite differences, for DOP853 and for the
+Magnus CFET8 stepper.
 
 Loss L = sum_i W_i . S_i(final) with fixed random weights W.  The GPU
 gradient (st_adjoint_record + st_adjoint_backward through the torch Function)
 is compared with central finite differences of the ORACLE (the reference
-algorithm on the CPU) run with its accepted DOP853 step sequence frozen to that
+algorithm on the CPU) run with its accepted step sequence frozen to that
 of the unperturbed run, which is the derivative the discrete adjoint computes.
 Bar: 1e-6 relative per parameter.  Steps: relative 1e-6 of |B0| for B0 (the
 spec's step) and for the pulse; the gradient tensor and E make up only 1e-5 to
@@ -27,11 +28,11 @@ from spintrack.adjoint import NUM_THETA, THETA_NAMES, precession_phase, theta_of
 pytestmark = pytest.mark.gpu
 
 
-def adj_options(n=8, tf=0.1, pulse=False, seed=5):
+def adj_options(n=8, tf=0.1, pulse=False, seed=5, integrator=0):
     g = np.random.default_rng(3).normal(0.0, 1e-9, 9)
     kw = dict(numParticles=n, dist="M", T=4.2, diffuse=0.0, gas_coll=False, gravity=True, Gx=g[0:3], Gy=g[3:6],
               Gz=g[6:9], E=(0.0, 0.0, 75e5), B0=(3e-6, 0.0, 0.0), yi=(0.0, 0.0, 1.0), tf=tf, ioutInt=0.05, seed=seed,
-              rtol=1e-12, atol=1e-12, h=1e-3, hmax=1.0, hmin=1e-8)
+              rtol=1e-12, atol=1e-12, h=1e-3, hmax=1.0, hmin=1e-8, integratorType=integrator)
     if pulse:
         kw.update(a=5e-6, w=2 * math.pi * 1000.0, hmax=1e-4)
     return st.derive(st.make_options(**kw))
@@ -87,9 +88,10 @@ def gpu_grad(opt, W, pulse):
     return g, S_np
 
 
+@pytest.mark.parametrize("integrator", [0, 2], ids=["dop853", "magnus"])
 @pytest.mark.parametrize("pulse", [False, True], ids=["static", "pulse"])
-def test_adjoint_matches_frozen_step_fd(gpu, oracle, pulse):
-    opt = adj_options(pulse=pulse)
+def test_adjoint_matches_frozen_step_fd(gpu, oracle, pulse, integrator):
+    opt = adj_options(pulse=pulse, integrator=integrator)
     W = np.random.default_rng(11).normal(size=(opt.numParticles, 3))
     g, S = gpu_grad(opt, W, pulse)
     fd, base = frozen_fd(oracle, opt, W, pulse)
@@ -107,9 +109,10 @@ def test_adjoint_matches_frozen_step_fd(gpu, oracle, pulse):
     assert not bad, "\n".join(rows)
 
 
-def test_record_pass_is_the_forward_map(gpu):
+@pytest.mark.parametrize("integrator", [0, 2], ids=["dop853", "magnus"])
+def test_record_pass_is_the_forward_map(gpu, integrator):
     """st_adjoint_record advances particles exactly as st_run_windows."""
-    opt = adj_options(n=64, tf=0.2)
+    opt = adj_options(n=64, tf=0.2, integrator=integrator)
     nw = st.num_windows(opt)
     with st.Particles(opt) as p, st.Particles(opt) as q:
         p.init_particles()
@@ -162,12 +165,13 @@ def _grad_with_budget(p, nw, w, tape_bytes, every):
     return out.cpu().numpy(), p.adjoint_stats()
 
 
-def test_backward_is_independent_of_the_tape_budget(gpu):
+@pytest.mark.parametrize("integrator", [0, 2], ids=["dop853", "magnus"])
+def test_backward_is_independent_of_the_tape_budget(gpu, integrator):
     """The same gradients whether the record pass's tape fits (no replay), or
     window chunks are replayed from state checkpoints, or a single window is
     replayed in particle groups; final states identical in every case."""
     import torch
-    opt = adj_options(n=16, tf=0.2)
+    opt = adj_options(n=16, tf=0.2, integrator=integrator)
     nw = st.num_windows(opt)
     assert nw == 4
     dev = torch.device("cuda", 0)
