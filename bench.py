@@ -257,6 +257,9 @@ WORKLOADS = {
                    "0.0125 s, RKF45 rtol 1e-3 tf 0.005 s, RKF45 with quaternions rtol 1e-6 tf 2.5e-4 s (the RKF45 "
                    "pair's error estimates are the whole increment and the last stage's rotation: they accept "
                    "only steps of ~3 us and ~0.1 us, and tighter tolerances fail with h < hmin), one window each",
+    "adjoint-magnus": "adjoint of the Magnus CFET8 stepper: 65,536 particles, MB 4.2 K, specular walls, gravity, gas "
+                      "off, G ~ N(0,1e-9) T/m, E = (0,0,75e5), B0 = (3e-6,0,0), integratorType 2, rtol 1e-12, "
+                      "tf = 1 s, ioutInt 0.5 s; gradients of <Sx>, <Sy> and the mean precession phase",
     "dressing-grid": "dressing sensitivity: 8 x 8 grid a in [1,10] uT, w in 2 pi [500,2000] rad/s as 64 parameter "
                      "sets x 4096 particles in one context, otherwise as 'dressing' with tf = 0.2 s; d<P>/d(a, w) of "
                      "the polarisation P = |<S>| per grid point from one record + one backward pass",
@@ -381,11 +384,13 @@ def run_workload(args):
         return line
 
     tape_bytes = 0
-    if args.workload in ("adjoint50", "adjoint-small"):
+    if args.workload in ("adjoint50", "adjoint-small", "adjoint-magnus"):
         g = np.random.default_rng(0).normal(0.0, 1e-9, 9)
         small = args.workload == "adjoint-small"
-        opt = _set_options(65536, 0.05 if small else 50.0, diffuse=0.0, Gx=tuple(g[0:3]), Gy=tuple(g[3:6]),
-                           Gz=tuple(g[6:9]), ioutInt=0.05 if small else 0.5)
+        magnus = args.workload == "adjoint-magnus"
+        tf = 0.05 if small else (1.0 if magnus else 50.0)
+        opt = _set_options(65536, tf, diffuse=0.0, Gx=tuple(g[0:3]), Gy=tuple(g[3:6]), Gz=tuple(g[6:9]),
+                           ioutInt=0.05 if small else 0.5, integratorType=2 if magnus else 0)
         sets = [opt]
         tape_bytes = 3_000_000_000 if small else 0
     else:
