@@ -216,15 +216,23 @@ static size_t variant_smem(int v) {
   return batched_smem(x.block, x.qcap, x.stages);
 }
 
-// Opt the kernels that need more than 48 KiB of dynamic shared memory in, once.
+// Function attributes are set per device: remember which devices have them
+// (devices beyond the table are set every time).
+constexpr int kAttrDevices = 16;
+static int current_device() {
+  int d = 0;
+  return cudaGetDevice(&d) == cudaSuccess ? d : kAttrDevices;
+}
+
+// Opt the kernels that need more than 48 KiB of dynamic shared memory in, once per device.
 static cudaError_t ensure_smem(int v, bool gas, bool ext) {
-  static bool done[kNumVariants][3] = {};
-  const int k = ext ? 2 : (gas ? 1 : 0);
-  if (done[v][k]) return cudaSuccess;
+  static bool done[kAttrDevices][kNumVariants][3] = {};
+  const int k = ext ? 2 : (gas ? 1 : 0), d = current_device();
+  if (d < kAttrDevices && done[d][v][k]) return cudaSuccess;
   const size_t sm = variant_smem(v);
   cudaError_t e = cudaSuccess;
   if (sm > 0) e = cudaFuncSetAttribute(variant_fn(v, gas, ext), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e == cudaSuccess) done[v][k] = true;
+  if (e == cudaSuccess && d < kAttrDevices) done[d][v][k] = true;
   return e;
 }
 
@@ -276,12 +284,12 @@ static const void* tape_fn(bool gas, bool ext) {
 static size_t tape_smem() { return batched_smem(kTapeBlock, kTapeQcap, 0); }
 
 static cudaError_t tape_ensure_smem(bool gas, bool ext) {
-  static bool done[3] = {};
-  const int k = ext ? 2 : (gas ? 1 : 0);
-  if (done[k]) return cudaSuccess;
+  static bool done[kAttrDevices][3] = {};
+  const int k = ext ? 2 : (gas ? 1 : 0), d = current_device();
+  if (d < kAttrDevices && done[d][k]) return cudaSuccess;
   cudaError_t e =
       cudaFuncSetAttribute(tape_fn(gas, ext), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tape_smem());
-  if (e == cudaSuccess) done[k] = true;
+  if (e == cudaSuccess && d < kAttrDevices) done[d][k] = true;
   return e;
 }
 
