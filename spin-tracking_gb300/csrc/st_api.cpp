@@ -13,6 +13,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -1534,8 +1535,13 @@ struct TuneKey {
     return ntypes_mask != o.ntypes_mask ? ntypes_mask < o.ntypes_mask : log2n < o.log2n;
   }
 };
+// Process-wide choices, shared by contexts on any host thread.
 std::map<TuneKey, st_launch_config>& tune_cache() {
   static std::map<TuneKey, st_launch_config> m;
+  return m;
+}
+std::mutex& tune_mutex() {
+  static std::mutex m;
   return m;
 }
 
@@ -1547,10 +1553,13 @@ int autotune(st_ctx* c) {
   }
   const int ext = ctx_any_ext(c) ? 1 : 0;
   while ((int64_t(1) << key.log2n) < c->n) ++key.log2n;
-  auto it = tune_cache().find(key);
-  if (it != tune_cache().end()) {
-    c->lc = it->second;
-    return ST_OK;
+  {
+    std::lock_guard<std::mutex> lock(tune_mutex());
+    auto it = tune_cache().find(key);
+    if (it != tune_cache().end()) {
+      c->lc = it->second;
+      return ST_OK;
+    }
   }
   const int nv = st::persistent_variant_count();
   // Sample: every set represented, about four particles per lane of the
@@ -1599,6 +1608,7 @@ int autotune(st_ctx* c) {
   }
   st_destroy(s);
   c->lc = best_cfg;
+  std::lock_guard<std::mutex> lock(tune_mutex());
   tune_cache()[key] = best_cfg;
   return ST_OK;
 }
