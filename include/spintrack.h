@@ -291,6 +291,12 @@ int st_ensemble_stats(st_ctx *ctx, const void *snap, int set, st_ensemble *out);
  * DFMA chains per thread on every SM.  No counterpart in the reference; it is
  * the roofline denominator for the step kernels, which are FP64-pipe bound. */
 int st_probe_fp64_peak(int device, double *tflops);
+/* The trajectory's correctly rounded libm replacements (log, sin, cos, acos;
+ * their results equal the host C library's wherever those are correctly
+ * rounded), evaluated over n doubles of a device array x into device array y
+ * on the current device, synchronously: fn 0 log, 1 sin, 2 cos, 3 acos.
+ * For tests; no reference counterpart. */
+int st_crmath_eval(int fn, const double *x, double *y, int64_t n);
 
 /* ---- driver: mainAnalysis (src/simulation.cpp:8-96) -------------------- */
 /* Derive tc/sqrtKT_m, create, init, write the options header and the t0

@@ -6,8 +6,10 @@
 //  * Trajectory and RNG code reproduces the reference's doubles bit for bit
 //    (same operation order, no FMA contraction: every add/mul/div/sqrt is an
 //    explicit round-to-nearest intrinsic), so event times, bounce/collision
-//    counts and RNG draws match the CPU build exactly.  Only CUDA's log / acos /
-//    cos / sin may differ from libm by an ulp.
+//    counts and RNG draws match the CPU build exactly.  Only its log, acos, cos
+//    and sin may differ from the host C library by an ulp (CUDA's), unless
+//    ST_TRAJ_CORRECTLY_ROUNDED selects the correctly rounded ones of
+//    st_crmath.cuh (st_fields.cuh).
 //  * The spin steppers are restated for the FP64 pipe: FMA-contracted stage
 //    sums, the field as a polynomial in segment time, reciprocal-form error
 //    weights and step controller.  Results agree with the reference to the
@@ -19,6 +21,33 @@
 #include "st_internal.h"
 #include "st_fields.cuh"
 #include "st_tableau.h"
+#include "st_crmath.cuh"
+
+namespace st {
+// The trajectory's transcendental functions (ST_TRAJ_CORRECTLY_ROUNDED, st_fields.cuh).
+__device__ __forceinline__ double traj_log(double x) {
+#if ST_TRAJ_CORRECTLY_ROUNDED
+  return crm::cr_log(x);
+#else
+  return log(x);
+#endif
+}
+__device__ __forceinline__ double traj_acos(double x) {
+#if ST_TRAJ_CORRECTLY_ROUNDED
+  return crm::cr_acos(x);
+#else
+  return acos(x);
+#endif
+}
+__device__ __forceinline__ void traj_sincos(double x, double& s, double& c) {
+#if ST_TRAJ_CORRECTLY_ROUNDED
+  crm::cr_sincos(x, s, c);
+#else
+  s = sin(x);
+  c = cos(x);
+#endif
+}
+}  // namespace st
 
 namespace st {
 
@@ -113,13 +142,13 @@ __device__ __forceinline__ double rng_normal(Rng& r, double mean, double sd) {
     v = xadd(xmul(rng_uniform(r), 2.0), -1.0);
     s = xadd(xmul(u, u), xmul(v, v));
   } while (s >= 1.0 || s == 0.0);
-  s = xsqrt(xdiv(xmul(-2.0, log(s)), s));
+  s = xsqrt(xdiv(xmul(-2.0, traj_log(s)), s));
   r.spare = xmul(v, s);
   r.has = true;
   return xadd(mean, xmul(xmul(sd, u), s));
 }
 __device__ __forceinline__ double rng_exponential(Rng& r, double tc) {
-  return xmul(-tc, log(xsub(1.0, rng_uniform(r))));
+  return xmul(-tc, traj_log(xsub(1.0, rng_uniform(r))));
 }
 
 // Seeding of initParticlesCPU (src/particle.cpp:648-663): splitmix64 of the
@@ -248,8 +277,10 @@ struct DiffuseDefer {
 
 // New velocity of a cosine-law diffuse reflection off wall w (src/particle.cpp:309-328).
 __device__ __forceinline__ void diffuse_velocity(PState& p, double su, double theta, double speed, char w) {
-  const double phi = acos(su);
-  const double cp = cos(phi), sp = sin(phi), ct = cos(theta), stt = sin(theta);
+  const double phi = traj_acos(su);
+  double cp, sp, ct, stt;
+  traj_sincos(phi, sp, cp);
+  traj_sincos(theta, stt, ct);
   if (w == 'x') {
     p.vx = xmul(xmul(xmul(-1.0, sgn1(p.vx)), speed), cp);
     p.vy = xmul(xmul(-speed, sp), ct);

@@ -16,6 +16,17 @@
 // in pos, set ST_GRAD_IS_LINEAR to 0: every stage then evaluates the hook.
 // Likewise ST_PULSE_IS_Z_COS selects the built-in a*cos(w t) z pulse; set it to
 // 0 after editing st_pulse.
+//
+// ST_TRAJ_CORRECTLY_ROUNDED 1 makes the trajectory's log, acos, cos and sin
+// the correctly rounded ones of st_crmath.cuh (equal to the host C library's
+// results wherever those are correctly rounded) instead of CUDA's (within an
+// ulp).  Runs with gas collisions and diffuse walls then stay bit-exact with
+// the CPU reference for longer: on the reference's own params.txt (gas at
+// 0.4 K, diffuse 0.3, 1,024 particles, 10 s) the first particle's counts
+// diverge after 4.5 s instead of 3 s, and 462 instead of more than 2,000
+// (particle, snapshot) pairs carry a differing count.  It costs ~20% of the
+// throughput at diffuse 0.1 (the deferred diffuse reflections run the longer
+// code with few lanes active), so it is off by default.
 #pragma once
 
 #include "st_internal.h"
@@ -25,6 +36,9 @@
 #endif
 #ifndef ST_PULSE_IS_Z_COS
 #define ST_PULSE_IS_Z_COS 1
+#endif
+#ifndef ST_TRAJ_CORRECTLY_ROUNDED
+#define ST_TRAJ_CORRECTLY_ROUNDED 0
 #endif
 
 namespace st {

@@ -145,6 +145,7 @@ struct TapeArgs {
   long long* error;               // kTapeErrorSlots: first inconsistency found (code, particle, cursors)
 };
 // The trajectory-ahead kernel with its tape switch on (st_kernels.cu).
+int launch_crmath_eval(int fn, const double* x, double* y, int64_t n, void* stream);
 int launch_tape_record(const RunArgs& a, const TapeArgs& t, int blocks, void* stream);  // a.any_ext: Magnus
 int tape_record_block();
 int tape_record_max_blocks_per_sm(int ext);

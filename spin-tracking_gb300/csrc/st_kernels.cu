@@ -68,6 +68,28 @@ __global__ void k_pack(RunArgs a, int slot) {
   reinterpret_cast<int32_t*>(b + o[14])[i] = a.s.turns[i];
 }
 
+// ------------------------------------------------------------------ libm replacements
+// The trajectory's correctly rounded functions over an array (for tests):
+// fn 0 log, 1 sin, 2 cos, 3 acos.
+__global__ void k_crmath_eval(int fn, const double* x, double* y, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  double s, c;
+  switch (fn) {
+    case 0: y[i] = crm::cr_log(v); break;
+    case 1: crm::cr_sincos(v, s, c); y[i] = s; break;
+    case 2: crm::cr_sincos(v, s, c); y[i] = c; break;
+    default: y[i] = crm::cr_acos(v); break;
+  }
+}
+
+int launch_crmath_eval(int fn, const double* x, double* y, int64_t n, void* stream) {
+  if (n <= 0) return 0;
+  k_crmath_eval<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(fn, x, y, n);
+  return (int)cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ FP64 peak probe
 // Eight independent DFMA chains per thread: the FP64 pipe's issue rate, the
 // denominator of the step kernels' roofline.

@@ -117,6 +117,7 @@ _SIGS = {
     "st_launch_variant_name": (c_char_p, [c_int]),
     "st_get_counters": (c_int, [c_void_p, POINTER(Counters)]),
     "st_main_analysis": (c_int, [POINTER(Options), c_char_p, c_int, c_int, POINTER(c_double)]),
+    "st_crmath_eval": (c_int, [c_int, c_void_p, c_void_p, ctypes.c_int64]),
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),
     "st_adjoint_record": (c_int, [c_void_p, c_int, c_size_t, c_int]),
     "st_adjoint_get_stats": (c_int, [c_void_p, POINTER(AdjointStats)]),
