@@ -151,3 +151,45 @@ def test_main_analysis_refuses_hdf5_names_before_device_work(stlib, tmp_path, na
     assert stlib.st_main_analysis(ctypes.byref(o), str(path).encode(), 0, 1, None) == _capi.ST_ERR_UNSUPPORTED
     assert b"HDF5" in stlib.st_last_error()
     assert not path.exists()
+
+
+def _random_params(rng):
+    """A well-formed params file over random keys, formats and values."""
+    scal = ["tf", "t0", "ioutInt", "rtol", "atol", "h", "hmax", "hmin", "T", "V", "m", "gamma", "diffuse",
+            "maxPosStep", "a", "w", "beta", "safe", "fac1", "fac2", "uround"]
+    ints = ["numParticles", "numPerGPUBlock", "seed", "nmax", "integratorType", "iout"]
+    bools = ["gas_coll", "gravity", "fixedStepSize", "keepStepSize"]
+    vecs = ["L", "B0", "E", "yi", "Gx", "Gy", "Gz"]
+    def num():
+        v = rng.normal() * 10.0 ** rng.integers(-12, 9)
+        return rng.choice([repr(float(v)), f"{v:.6e}", f"{v:g}", f" {v:.3E} "])
+    lines = []
+    for _ in range(rng.integers(1, 25)):
+        kind = rng.integers(0, 5)
+        if kind == 0:
+            lines.append(f"{rng.choice(scal)}, {num()}")
+        elif kind == 1:
+            lines.append(f"{rng.choice(ints)}, {int(rng.integers(-5, 100000))}")
+        elif kind == 2:
+            lines.append(f"{rng.choice(bools)}, {rng.choice(['true', 'false', 'True', 'FALSE', '0', '1'])}")
+        elif kind == 3:
+            lines.append(f" {rng.choice(vecs)} ,{num()}, {num()},{num()}")
+        else:
+            lines.append(f"dist, {rng.choice(['C', 'M', 'Maxwell', 'Constant'])}")
+    return "\n".join(lines) + "\n"
+
+
+def test_parse_params_equals_oracle_on_random_files(stlib, oracle, tmp_path):
+    """The library's params parser and the oracle's (the reference's
+    optionParser restated) give the same 440-byte options image on random
+    well-formed files: keys in any order and repetition, numbers in every
+    format stod accepts, booleans in boolalpha's cases, padded fields."""
+    import numpy as np
+    rng = np.random.default_rng(17)
+    for k in range(200):
+        path = tmp_path / f"r{k}.params"
+        path.write_text(_random_params(rng))
+        a = Options()
+        assert stlib.st_parse_params(str(path).encode(), ctypes.byref(a)) == 0, path.read_text()
+        b = oracle.parse_file(path, derive=False)
+        assert bytes(a) == bytes(b), path.read_text()
