@@ -22,6 +22,9 @@
 //                                     integrateRK45Quaternion (:441),
 //                                     integrateRKF45 (:339),
 //                                     integrateRKF45Quaternion (:530) likewise
+//   ref_probe options PARAMS         the options image optionParser produced
+//                                     (src/optionsParser.cpp:177), derived as
+//                                     mainAnalysis does, as hex bytes
 //   ref_probe events PARAMS NSEG      per particle after init: NSEG rounds of
 //                                     calc_next_collision_time + update +
 //                                     sanity_check (src/particle.cpp:121-444)
@@ -77,6 +80,13 @@ int main(int argc, char** argv) {
   if (argc < 3) { std::fprintf(stderr, "usage: ref_probe CMD PARAMS ...\n"); return 2; }
   const char* cmd = argv[1];
   options opt = load(argv[2]);
+  if (!std::strcmp(cmd, "options")) {  // the parsed (and derived) options image, as hex bytes
+    const unsigned char* b = reinterpret_cast<const unsigned char*>(&opt);
+    std::printf("options ");
+    for (size_t k = 0; k < sizeof(opt); ++k) std::printf("%02x", b[k]);
+    std::printf("\n");
+    return 0;
+  }
   if (!std::strcmp(cmd, "init") || !std::strcmp(cmd, "draws") || !std::strcmp(cmd, "events")) {
     Arrays a(opt.numParticles);
     init_all(opt, a);

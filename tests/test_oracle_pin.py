@@ -218,3 +218,25 @@ def test_golden_cases_exercise_the_paths():
         seen["bounce"] += int(last["n_bounce"].sum())
         seen["fail"] += int((last["fail"] != 0).sum())
     assert seen["gas"] > 100 and seen["bounce"] > 1000 and seen["fail"] > 0
+
+
+def test_parser_matches_reference_on_random_files(oracle, tmp_path):
+    """optionParser (the reference's own, through oracle/_ref/ref_probe) and the
+    oracle's restatement give the same options image, derived fields
+    included, on 100 random well-formed params files (keys in any order and
+    repetition, every number format stod accepts, boolalpha cases)."""
+    import subprocess
+    from pathlib import Path
+    import numpy as np
+    from test_host_abi import _random_params
+    probe = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_probe"
+    if not probe.exists():
+        pytest.skip("the reference build (oracle/_ref) is not present on this machine")
+    rng = np.random.default_rng(29)
+    for k in range(100):
+        path = tmp_path / f"r{k}.params"
+        path.write_text(_random_params(rng))
+        out = subprocess.run([str(probe), "options", str(path)], capture_output=True, text=True, timeout=60).stdout
+        ref = bytes.fromhex(out.strip().splitlines()[-1].split()[1])
+        ours = bytes(oracle.parse_file(path, derive=True))
+        assert header_equal(ours, ref), path.read_text()
