@@ -240,3 +240,64 @@ def test_parser_matches_reference_on_random_files(oracle, tmp_path):
         ref = bytes.fromhex(out.strip().splitlines()[-1].split()[1])
         ours = bytes(oracle.parse_file(path, derive=True))
         assert header_equal(ours, ref), path.read_text()
+
+
+def _check_events(oracle, params, text):
+    """Replay the reference's event lines (ref_probe events) with the oracle."""
+    opt = oracle.parse_file(params)
+    p = oracle.alloc(opt.numParticles)
+    try:
+        oracle.L.or_init(ctypes.byref(opt), ctypes.byref(p), 0)
+        i, nseg = 0, 0
+        for line in text.splitlines():
+            tok = line.split()
+            if not tok:
+                continue
+            if tok[0] == "p":
+                i = int(tok[1])
+                continue
+            oracle.L.or_event(ctypes.byref(opt), ctypes.byref(p), i, opt.tf)
+            assert p.coll_type[i] == tok[1].encode()
+            if tok[2] != "-":
+                assert p.wall_hit[i] == tok[2].encode()
+            assert int(p.stop[i]) == int(tok[3]) and p.fail[i] == int(tok[4])
+            vals = [hexf(x) for x in tok[5:14]]
+            assert p.t[i] == vals[1]
+            assert [p.pos[i].x, p.pos[i].y, p.pos[i].z] == vals[2:5]
+            assert [p.v[i].x, p.v[i].y, p.v[i].z] == vals[5:8]
+            assert p.next_gas[i] == vals[8]
+            assert p.rng[i].x == int(tok[14])
+            nseg += 1
+        return nseg
+    finally:
+        oracle.free(p)
+
+
+def test_events_match_reference_on_random_configurations(oracle, tmp_path):
+    """Trajectory events of the reference (ref_probe events) and of the oracle,
+    bit for bit, over 24 random configurations: box sizes, 'C' speeds and
+    'M' temperatures, gas on and off, diffuse fractions from 0 to 1, gravity
+    on and off, seeds."""
+    import subprocess
+    from pathlib import Path
+    import numpy as np
+    probe = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_probe"
+    if not probe.exists():
+        pytest.skip("the reference build (oracle/_ref) is not present on this machine")
+    rng = np.random.default_rng(41)
+    total = 0
+    for k in range(24):
+        L = rng.uniform(0.02, 0.5, 3)
+        dist = rng.choice(["C", "M"])
+        T = float(rng.choice([0.4, 1.0, 4.2]))
+        gas = bool(rng.random() < 0.5) and T < 4.0  # at 4.2 K the gas clock is picoseconds
+        text = (f"numParticles, 6\ndist, {dist}\nV, {rng.uniform(1, 10):.6g}\nT, {T}\n"
+                f"gas_coll, {'true' if gas else 'false'}\ndiffuse, {rng.uniform(0, 1):.6g}\n"
+                f"gravity, {'true' if rng.random() < 0.7 else 'false'}\nL, {L[0]:.6g}, {L[1]:.6g}, {L[2]:.6g}\n"
+                f"yi, 0, 0, 1\ntf, 1\nioutInt, 0.5\nseed, {int(rng.integers(0, 2**31))}\n")
+        params = tmp_path / f"e{k}.params"
+        params.write_text(text)
+        out = subprocess.run([str(probe), "events", str(params), "60"], capture_output=True, text=True,
+                             timeout=120).stdout
+        total += _check_events(oracle, params, out)
+    assert total > 24 * 6 * 30
