@@ -55,18 +55,18 @@ out.append("constexpr double kThirdHi = %s, kThirdLo = %s;" % (h(third[0]), h(th
 sixth = dd(mp.mpf(1) / 6)
 out.append("constexpr double kSixthHi = %s, kSixthLo = %s;" % (h(sixth[0]), h(sixth[1])))
 # pi/2 and pi/64 in three parts: 33 + 33 + 53 bits
-for name, v in (("kPio2", mp.pi / 2), ("kPio64", mp.pi / 64)):
+for name, v in (("kPio2", mp.pi / 2), ("kPio256", mp.pi / 256)):
     p1, rest = split(v, 33)
     p2, rest = split(rest, 33)
     p3 = float(rest)
     out.append("constexpr double %s1 = %s, %s2 = %s, %s3 = %s;" % (name, h(p1), name, h(p2), name, h(p3)))
-out.append("constexpr double kTwoOverPi = %s, kSixtyFourOverPi = %s;" % (h(float(2 / mp.pi)), h(float(64 / mp.pi))))
-# sin, cos of j pi / 64, j = 0..16
-out.append("// sin(j pi / 64), cos(j pi / 64), j = 0..16, as hi, lo.")
-sv = [dd(mp.sin(j * mp.pi / 64)) for j in range(17)]
-cv = [dd(mp.cos(j * mp.pi / 64)) for j in range(17)]
-out.append("static __device__ const double kSinA[17][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in sv) + "};")
-out.append("static __device__ const double kCosA[17][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in cv) + "};")
+out.append("constexpr double kTwoOverPi = %s, k256OverPi = %s;" % (h(float(2 / mp.pi)), h(float(256 / mp.pi))))
+# sin, cos of j pi / 256, j = 0..64
+out.append("// sin(j pi / 256), cos(j pi / 256), j = 0..64, as hi, lo.")
+sv = [dd(mp.sin(j * mp.pi / 256)) for j in range(65)]
+cv = [dd(mp.cos(j * mp.pi / 256)) for j in range(65)]
+out.append("static __device__ const double kSinA[65][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in sv) + "};")
+out.append("static __device__ const double kCosA[65][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in cv) + "};")
 out.append("}  // namespace crm")
 out.append("}  // namespace st")
 print("\n".join(out))

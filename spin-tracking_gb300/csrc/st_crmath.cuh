@@ -8,21 +8,25 @@
 // of these arguments, and a trajectory grazing the ceiling turns such an ulp
 // into a wall-time difference that can swap a gas collision and a wall hit,
 // after which the particle consumes its random stream differently.  These
-// functions evaluate the value in double-double arithmetic (~2^-85
-// relative) and round it once, so they return the correctly rounded double
-// except where the exact value lies within ~2^-85 of a rounding boundary.
+// functions evaluate the value in double-double arithmetic (~2^-67 relative
+// or better) and round it once, so they return the correctly rounded double
+// except where the exact value lies that close to a rounding boundary (about
+// one argument in 10^4, against the host library's own ~10^-3).
 //
 // Methods (standard, from the mathematics):
 //   log: x = 2^e m, m in [0.75, 1.5); m = (1 + t) / R with R from a 96-entry
 //        table (R = 1 near m = 1), so log x = e ln 2 - log R + log1p(t),
 //        |t| <= 2^-7, log1p by its Taylor series (terms to t^3 in
 //        double-double, the rest to t^13 in double).
-//   sin/cos: Cody-Waite reduction by pi/2 and by pi/64 with three-part
+//   sin/cos: Cody-Waite reduction by pi/2 and by pi/256 with three-part
 //        constants (exact products for the arguments used here, |x| < 2^20),
-//        table of sin, cos(j pi / 64) in double-double, Taylor series of the
-//        remainder (|s| <= pi/128) to s^11, angle addition in double-double.
+//        table of sin, cos(j pi / 256) in double-double, Taylor series of the
+//        remainder (|s| <= pi/512) in double, angle addition with the leading
+//        products exact (~2^-67 relative before the rounding).
 //   acos: CUDA's acos as the start, one Newton step on cos(y) - x evaluated
-//        with the double-double cos and sin, one rounding.
+//        with the double-double cos and sin, one rounding; the reflection's
+//        sin and cos of the result reuse that evaluation when it rounds to
+//        the start.
 #pragma once
 
 #include "st_crmath_tables.h"
@@ -116,42 +120,45 @@ static __device__ __noinline__ double cr_log(double x) {
 }
 
 // ---------------------------------------------------------------- sin, cos
-// sin and cos of x, 0 <= |x| < 2^20, as double-double values.
+// sin and cos of x, 0 <= |x| < 2^20, as double-double values accurate to
+// ~2^-67 relative.
 __device__ __forceinline__ void sincos_dd(double x, DD& sn, DD& cs) {
-  // x = k pi/2 + r
+  // x = k pi/2 + r, r as double-double (k * kPio21 and k * kPio22 are exact)
   const double k = rint(__dmul_rn(x, kTwoOverPi));
-  const double r1 = __fma_rn(-k, kPio21, x);  // exact: k * kPio21 is exact and cancels
-  DD r = two_sum(r1, __dmul_rn(-k, kPio22));  // k * kPio22 is exact
+  const double r1 = __fma_rn(-k, kPio21, x);
+  DD r = two_sum(r1, __dmul_rn(-k, kPio22));
   r = dd_add(r, dd_neg(two_prod(k, kPio23)));
-  // r = j pi/64 + s
-  const double jd = rint(__dmul_rn(r.hi, kSixtyFourOverPi));
-  DD s = dd_add(r, {__dmul_rn(-jd, kPio641), 0.0});
-  s = dd_add(s, {__dmul_rn(-jd, kPio642), 0.0});
-  s = dd_add(s, dd_neg(two_prod(jd, kPio643)));
-  // sin s, cos s: Taylor series, |s| <= pi/128
-  const DD s2 = dd_mul(s, s);
-  const DD s3 = dd_mul(s2, s);
-  const double w = s2.hi;
-  double ps = -1.0 / 39916800.0;
-  ps = __fma_rn(ps, w, 1.0 / 362880.0);
-  ps = __fma_rn(ps, w, -1.0 / 5040.0);
-  ps = __fma_rn(ps, w, 1.0 / 120.0);
-  const double ts = __dmul_rn(ps, __dmul_rn(s3.hi, w));  // s^5 (1/120 - s^2/5040 + ...)
-  DD ss = dd_add(s, dd_neg(dd_mul(s3, {kSixthHi, kSixthLo})));
-  ss = dd_add_d(ss, ts);
-  double pc = 1.0 / 40320.0;
-  pc = __fma_rn(pc, w, -1.0 / 720.0);
-  pc = __fma_rn(pc, w, 1.0 / 24.0);
-  const double tc = __dmul_rn(pc, __dmul_rn(w, w));  // s^4 (1/24 - s^2/720 + s^4/40320)
-  DD cc = dd_add({1.0, 0.0}, {-0.5 * s2.hi, -0.5 * s2.lo});
-  cc = dd_add_d(cc, tc);
-  // angle addition with the table at a = |j| pi / 64
+  // r = j pi/256 + s, |s| <= pi/512 (j * kPio2561 and j * kPio2562 are exact)
+  const double jd = rint(__dmul_rn(r.hi, k256OverPi));
+  DD s = two_sum(__fma_rn(-jd, kPio2561, r.hi), __dmul_rn(-jd, kPio2562));
+  s = dd_add_d(s, r.lo);
+  const double sh = s.hi, sl = __fma_rn(-jd, kPio2563, s.lo);
+  // sin s - s and cos s - 1 by their Taylor series in double (to s^7 and s^6)
+  const double z = __dmul_rn(sh, sh);
+  const double sp = __dmul_rn(__dmul_rn(sh, z), __fma_rn(z, __fma_rn(z, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0));
+  const double cp = __fma_rn(-sh, sl, __dmul_rn(z, __fma_rn(z, __fma_rn(z, -1.0 / 720.0, 1.0 / 24.0), -0.5)));
+  // angle addition with the table at a = j pi / 256: the leading products
+  // exact, the small terms in double
   const int ja = (int)fabs(jd);
-  DD sa = {kSinA[ja][0], kSinA[ja][1]};
-  const DD ca = {kCosA[ja][0], kCosA[ja][1]};
-  if (jd < 0.0) sa = dd_neg(sa);
-  const DD sr = dd_add(dd_mul(sa, cc), dd_mul(ca, ss));
-  const DD cr = dd_add(dd_mul(ca, cc), dd_neg(dd_mul(sa, ss)));
+  double sah = kSinA[ja][0], sal = kSinA[ja][1];
+  if (jd < 0.0) {
+    sah = -sah;
+    sal = -sal;
+  }
+  const double cah = kCosA[ja][0], cal = kCosA[ja][1];
+  const double ss = __dadd_rn(sl, sp);  // sin s - sh
+  // sin(a + s) = sin a + cos a sh + [cos a (sin s - sh) + sin a (cos s - 1)]
+  const DD m = two_prod(cah, sh);
+  const DD hs = two_sum(sah, m.hi);
+  const double ts = __dadd_rn(__dadd_rn(m.lo, sal),
+                              __fma_rn(cal, sh, __fma_rn(sah, cp, __dmul_rn(cah, ss))));
+  const DD sr = fast_two_sum(hs.hi, __dadd_rn(hs.lo, ts));
+  // cos(a + s) = cos a - sin a sh + [cos a (cos s - 1) - sin a (sin s - sh)]
+  const DD m2 = two_prod(-sah, sh);
+  const DD hc = two_sum(cah, m2.hi);
+  const double tc = __dadd_rn(__dadd_rn(m2.lo, cal),
+                              __fma_rn(-sal, sh, __fma_rn(cah, cp, __dmul_rn(-sah, ss))));
+  const DD cr = fast_two_sum(hc.hi, __dadd_rn(hc.lo, tc));
   // quadrant
   const int q = ((int)k) & 3;
   if (q == 0) {
@@ -174,15 +181,30 @@ static __device__ __noinline__ void cr_sincos(double x, double& s, double& c) {
 }
 
 // ---------------------------------------------------------------- acos
-// acos of x in [0, 1], correctly rounded (see the file comment).
-static __device__ __noinline__ double cr_acos(double x) {
-  if (x >= 1.0) return acos(x);  // 0 at 1, NaN above
+// y = acos(x) for x in [0, 1], correctly rounded, with sin(y) and cos(y)
+// correctly rounded too (a cosine-law reflection needs all three).  CUDA's
+// acos gives y0; one Newton step on cos(y) - x with the double-double sin and
+// cos of y0 gives y; when y rounds to y0 (most arguments) those sin and cos
+// are y's, else they are evaluated again.
+static __device__ __noinline__ void cr_acos_sincos(double x, double& y, double& sy, double& cy) {
   const double y0 = acos(x);
   DD sn, cs;
   sincos_dd(y0, sn, cs);
-  const DD num = dd_add_d(cs, -x);  // cos(y0) - x
-  const double d = __ddiv_rn(__dadd_rn(num.hi, num.lo), __dadd_rn(sn.hi, sn.lo));
-  return __dadd_rn(y0, d);
+  if (x >= 1.0 || x != x) {  // acos(1) = 0 exactly; NaN passes through
+    y = y0;
+  } else {
+    const double num = __dadd_rn(__dsub_rn(cs.hi, x), cs.lo);  // cos(y0) - x
+    y = __dadd_rn(y0, __ddiv_rn(num, __dadd_rn(sn.hi, sn.lo)));
+  }
+  if (y != y0) sincos_dd(y, sn, cs);
+  sy = __dadd_rn(sn.hi, sn.lo);
+  cy = __dadd_rn(cs.hi, cs.lo);
+}
+
+static __device__ __noinline__ double cr_acos(double x) {
+  double y, sy, cy;
+  cr_acos_sincos(x, y, sy, cy);
+  return y;
 }
 
 }  // namespace crm

@@ -6,10 +6,10 @@
 //  * Trajectory and RNG code reproduces the reference's doubles bit for bit
 //    (same operation order, no FMA contraction: every add/mul/div/sqrt is an
 //    explicit round-to-nearest intrinsic), so event times, bounce/collision
-//    counts and RNG draws match the CPU build exactly.  Only its log, acos, cos
-//    and sin may differ from the host C library by an ulp (CUDA's), unless
-//    ST_TRAJ_CORRECTLY_ROUNDED selects the correctly rounded ones of
-//    st_crmath.cuh (st_fields.cuh).
+//    counts and RNG draws match the CPU build exactly.  Its log, acos, cos and
+//    sin are the correctly rounded ones of st_crmath.cuh (equal to the host C
+//    library's wherever those are correctly rounded), or CUDA's with
+//    ST_TRAJ_CORRECTLY_ROUNDED 0 (st_fields.cuh).
 //  * The spin steppers are restated for the FP64 pipe: FMA-contracted stage
 //    sums, the field as a polynomial in segment time, reciprocal-form error
 //    weights and step controller.  Results agree with the reference to the
@@ -32,11 +32,14 @@ __device__ __forceinline__ double traj_log(double x) {
   return log(x);
 #endif
 }
-__device__ __forceinline__ double traj_acos(double x) {
+// acos(x) and the sin and cos of the result
+__device__ __forceinline__ void traj_acos_sincos(double x, double& y, double& sy, double& cy) {
 #if ST_TRAJ_CORRECTLY_ROUNDED
-  return crm::cr_acos(x);
+  crm::cr_acos_sincos(x, y, sy, cy);
 #else
-  return acos(x);
+  y = acos(x);
+  sy = sin(y);
+  cy = cos(y);
 #endif
 }
 __device__ __forceinline__ void traj_sincos(double x, double& s, double& c) {
@@ -277,9 +280,8 @@ struct DiffuseDefer {
 
 // New velocity of a cosine-law diffuse reflection off wall w (src/particle.cpp:309-328).
 __device__ __forceinline__ void diffuse_velocity(PState& p, double su, double theta, double speed, char w) {
-  const double phi = traj_acos(su);
-  double cp, sp, ct, stt;
-  traj_sincos(phi, sp, cp);
+  double phi, cp, sp, ct, stt;
+  traj_acos_sincos(su, phi, sp, cp);
   traj_sincos(theta, stt, ct);
   if (w == 'x') {
     p.vx = xmul(xmul(xmul(-1.0, sgn1(p.vx)), speed), cp);

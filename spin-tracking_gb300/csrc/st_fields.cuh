@@ -17,16 +17,16 @@
 // Likewise ST_PULSE_IS_Z_COS selects the built-in a*cos(w t) z pulse; set it to
 // 0 after editing st_pulse.
 //
-// ST_TRAJ_CORRECTLY_ROUNDED 1 makes the trajectory's log, acos, cos and sin
-// the correctly rounded ones of st_crmath.cuh (equal to the host C library's
-// results wherever those are correctly rounded) instead of CUDA's (within an
-// ulp).  Runs with gas collisions and diffuse walls then stay bit-exact with
-// the CPU reference for longer: on the reference's own params.txt (gas at
-// 0.4 K, diffuse 0.3, 1,024 particles, 10 s) the first particle's counts
-// diverge after 4.5 s instead of 3 s, and 462 instead of more than 2,000
-// (particle, snapshot) pairs carry a differing count.  It costs ~20% of the
-// throughput at diffuse 0.1 (the deferred diffuse reflections run the longer
-// code with few lanes active), so it is off by default.
+// ST_TRAJ_CORRECTLY_ROUNDED 1 (the default) makes the trajectory's log, acos,
+// cos and sin the correctly rounded ones of st_crmath.cuh, equal to the host
+// C library's results wherever those are correctly rounded, instead of
+// CUDA's (within an ulp; on 0.3% of gas-clock and 14-23% of reflection
+// arguments not the host's).  Gas-collision and diffuse-wall trajectories
+// then stay bit-exact with the CPU reference far longer: CUDA's functions
+// swap a bounce within 0.1 s on a diffuse-0.94 configuration and diverge
+// after 3 s on the reference's own params.txt.  The cost: ~7% of the
+// throughput at diffuse 0.1, ~24% on a gas-heavy parameter sweep.  Set it
+// to 0 for CUDA's functions.
 #pragma once
 
 #include "st_internal.h"
@@ -38,7 +38,7 @@
 #define ST_PULSE_IS_Z_COS 1
 #endif
 #ifndef ST_TRAJ_CORRECTLY_ROUNDED
-#define ST_TRAJ_CORRECTLY_ROUNDED 0
+#define ST_TRAJ_CORRECTLY_ROUNDED 1
 #endif
 
 namespace st {
