@@ -301,3 +301,46 @@ def test_events_match_reference_on_random_configurations(oracle, tmp_path):
                              timeout=120).stdout
         total += _check_events(oracle, params, out)
     assert total > 24 * 6 * 30
+
+
+@pytest.mark.parametrize("which", ["dop", "rk45", "magnus", "rk45q", "rkf45", "rkf45q"])
+def test_segment_steppers_match_reference_on_random_segments(oracle, tmp_path, which):
+    """Every stepper over 30 random ballistic segments (start time, length,
+    spin, position, velocity, initial step; with and without the dressing
+    pulse and gravity), the reference's own integrator (ref_probe) against the
+    oracle's, bit for bit: return code, spin and carried step."""
+    import subprocess
+    from pathlib import Path
+    import numpy as np
+    probe = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_probe"
+    if not probe.exists():
+        pytest.skip("the reference build (oracle/_ref) is not present on this machine")
+    rtol = {"dop": "1e-12", "rk45": "1e-12", "magnus": "1e-12", "rk45q": "1e-10", "rkf45": "1e-3", "rkf45q": "1e-6"}
+    itype = {"dop": 0, "rk45": 1, **EXT_TYPE}
+    fn = {"dop": oracle.L.or_integrate_dop, "rk45": oracle.L.or_integrate_rk45}.get(which, oracle.L.or_integrate_ext)
+    rng = np.random.default_rng(7 + itype[which])
+    for k in range(30):
+        pulse = rng.random() < 0.5
+        g = rng.normal(0.0, 1e-9, 9)
+        text = (f"rtol, {rtol[which]}\ngravity, {'true' if rng.random() < 0.7 else 'false'}\n"
+                f"B0, {rng.uniform(1e-6, 5e-6):.6g}, {rng.normal(0, 1e-7):.6g}, 0\nE, 0, 0, 75e5\n"
+                f"Gx, {g[0]:.6g}, {g[1]:.6g}, {g[2]:.6g}\nGy, {g[3]:.6g}, {g[4]:.6g}, {g[5]:.6g}\n"
+                f"Gz, {g[6]:.6g}, {g[7]:.6g}, {g[8]:.6g}\n" + ("a, 5e-6\nw, 6283.185307179586\nhmax, 1e-4\n" if pulse else ""))
+        params = tmp_path / f"s{k}.params"
+        params.write_text(text)
+        t0 = rng.uniform(0.0, 1.0)
+        length = 10.0 ** rng.uniform(-5, -2) if which in ("rk45", "rk45q", "rkf45q") else 10.0 ** rng.uniform(-4, -1)
+        y = rng.normal(size=3)
+        y /= np.linalg.norm(y)
+        f = lambda x: repr(float(x))  # noqa: E731
+        args = [f(t0), f(t0 + length), *map(f, y), *map(f, rng.uniform(-0.05, 0.05, 3)),
+                *map(f, rng.normal(0, 5, 3)), f(10.0 ** rng.uniform(-6, -3)), "0"]
+        out = subprocess.run([str(probe), which, str(params), *args], capture_output=True, text=True,
+                             timeout=120).stdout.split()
+        opt = oracle.parse_file(params)
+        opt.integratorType = itype[which]
+        v = [float(a) for a in args]
+        yy, p0, v0, h = Vec3(*v[2:5]), Vec3(*v[5:8]), Vec3(*v[8:11]), ctypes.c_double(v[11])
+        ret = fn(ctypes.byref(opt), v[0], v[1], ctypes.byref(yy), ctypes.byref(p0), ctypes.byref(v0), ctypes.byref(h))
+        assert ret == int(out[1]), (k, args)
+        assert [yy.x, yy.y, yy.z, h.value] == [hexf(x) for x in out[2:6]], (k, args)
