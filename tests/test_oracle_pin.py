@@ -344,3 +344,49 @@ def test_segment_steppers_match_reference_on_random_segments(oracle, tmp_path, w
         ret = fn(ctypes.byref(opt), v[0], v[1], ctypes.byref(yy), ctypes.byref(p0), ctypes.byref(v0), ctypes.byref(h))
         assert ret == int(out[1]), (k, args)
         assert [yy.x, yy.y, yy.z, h.value] == [hexf(x) for x in out[2:6]], (k, args)
+
+
+def test_init_and_draws_match_reference_on_random_configurations(oracle, tmp_path):
+    """initParticlesCPU and the draws after it (raw xoshiro outputs, Marsaglia
+    normals) for 20 random configurations: 'C' speeds (including 0, where
+    the reference still draws the three normals) and 'M' temperatures, gas on
+    and off, box sizes, seeds up to 2^32 - 1."""
+    import subprocess
+    from pathlib import Path
+    import numpy as np
+    probe = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_probe"
+    if not probe.exists():
+        pytest.skip("the reference build (oracle/_ref) is not present on this machine")
+    rng = np.random.default_rng(61)
+    for k in range(20):
+        L = rng.uniform(0.02, 0.5, 3)
+        V = 0.0 if k == 0 else float(rng.uniform(0.5, 10))
+        seed = int(rng.integers(0, 2**32)) if k % 2 else int(rng.integers(0, 100))
+        text = (f"numParticles, 7\ndist, {rng.choice(['C', 'M'])}\nV, {V!r}\nT, {rng.choice([0.4, 1.3, 4.2])}\n"
+                f"gas_coll, {rng.choice(['true', 'false'])}\nL, {L[0]!r}, {L[1]!r}, {L[2]!r}\nseed, {seed}\n")
+        params = tmp_path / f"i{k}.params"
+        params.write_text(text)
+        opt = oracle.parse_file(params)
+        p = oracle.alloc(opt.numParticles)
+        try:
+            oracle.L.or_init(ctypes.byref(opt), ctypes.byref(p), 0)
+            out = subprocess.run([str(probe), "init", str(params)], capture_output=True, text=True, timeout=60).stdout
+            for tok in (l.split() for l in out.splitlines() if l.startswith("p ")):
+                i = int(tok[1])
+                vals = [hexf(x) for x in tok[2:9]]
+                assert [p.pos[i].x, p.pos[i].y, p.pos[i].z] == vals[0:3], (k, text)
+                assert [p.v[i].x, p.v[i].y, p.v[i].z] == vals[3:6], (k, text)
+                assert p.next_gas[i] == vals[6]
+                r = p.rng[i]
+                assert [r.x, r.y, r.z, r.w] == [int(x) for x in tok[9:13]]
+            out = subprocess.run([str(probe), "draws", str(params), "12"], capture_output=True, text=True,
+                                 timeout=60).stdout
+            for tok in (l.split() for l in out.splitlines() if l.startswith("p ")):
+                i = int(tok[1])
+                r = Rng.from_buffer_copy(bytes(p.rng[i]))
+                raw = [oracle.L.or_xoshiro(ctypes.byref(r)) for _ in range(12)]
+                assert raw == [int(x) for x in tok[2:14]], (k, text)
+                nrm = [oracle.L.or_normal(ctypes.byref(r), 0.0, 1.0) for _ in range(12)]
+                assert nrm == [hexf(x) for x in tok[14:26]], (k, text)
+        finally:
+            oracle.free(p)
