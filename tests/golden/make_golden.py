@@ -7,7 +7,8 @@ compiled unchanged against oracle/ref_stubs).  Writes, per case:
   <case>.bin             its output format 'A' file
 and probe vectors (C99 hex floats) from oracle/_ref/ref_probe:
   probe_init_<dist>.txt, probe_draws.txt, probe_events.txt, probe_dop.txt,
-  probe_rk45.txt
+  probe_rk45.txt, probe_magnus.txt, probe_rk45q.txt, probe_rkf45.txt,
+  probe_rkf45q.txt (single segments of every stepper)
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
