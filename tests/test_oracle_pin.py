@@ -390,3 +390,43 @@ def test_init_and_draws_match_reference_on_random_configurations(oracle, tmp_pat
                 assert nrm == [hexf(x) for x in tok[14:26]], (k, text)
         finally:
             oracle.free(p)
+
+
+def test_main_analysis_matches_reference_on_random_configurations(oracle, tmp_path):
+    """mainAnalysis end to end on 12 random configurations (all six
+    integrator types with tolerances each can meet, gas on and off, diffuse
+    fractions, gravity on and off, the dressing pulse): the reference build's
+    format-'A' file and the oracle's are equal bit for bit."""
+    import subprocess
+    from pathlib import Path
+    import numpy as np
+    exe = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "spintrack_ref"
+    if not exe.exists():
+        pytest.skip("the reference build (oracle/_ref) is not present on this machine")
+    rtol = {0: "1e-12", 1: "1e-12", 2: "1e-12", 3: "1e-10", 4: "1e-3", 5: "1e-6"}
+    tf = {0: 0.05, 1: 2e-4, 2: 0.05, 3: 0.01, 4: 0.004, 5: 4e-4}
+    rng = np.random.default_rng(83)
+    for k in range(12):
+        it = k % 6
+        L = rng.uniform(0.03, 0.4, 3)
+        T = float(rng.choice([0.4, 0.7, 4.2]))
+        g = rng.normal(0.0, 1e-9, 9)
+        lines = [f"numParticles, 8", f"dist, {rng.choice(['C', 'M'])}", f"V, {float(rng.uniform(2, 8))!r}", f"T, {T}",
+                 f"gas_coll, {'true' if (rng.random() < 0.5 and T < 4) else 'false'}",
+                 f"diffuse, {float(rng.uniform(0, 1))!r}", f"gravity, {'true' if rng.random() < 0.7 else 'false'}",
+                 f"L, {float(L[0])!r}, {float(L[1])!r}, {float(L[2])!r}",
+                 f"B0, {float(rng.uniform(1e-6, 5e-6))!r}, 0, 0", "E, 0, 0, 75e5",
+                 f"Gx, {float(g[0])!r}, {float(g[1])!r}, {float(g[2])!r}",
+                 f"Gy, {float(g[3])!r}, {float(g[4])!r}, {float(g[5])!r}",
+                 f"Gz, {float(g[6])!r}, {float(g[7])!r}, {float(g[8])!r}", "yi, 0, 0, 1", f"integratorType, {it}", f"rtol, {rtol[it]}",
+                 f"tf, {tf[it]!r}", f"ioutInt, {tf[it] / 2!r}", f"seed, {int(rng.integers(0, 2**31))}"]
+        if it in (0, 2) and rng.random() < 0.5:
+            lines += ["a, 5e-6", "w, 6283.185307179586", "hmax, 1e-4"]
+        params = tmp_path / f"m{k}.params"
+        params.write_text("\n".join(lines) + "\n")
+        ref_out, our_out = tmp_path / f"ref{k}.bin", tmp_path / f"ora{k}.bin"
+        subprocess.run([str(exe), str(params), str(ref_out)], capture_output=True, text=True, timeout=300)
+        oracle.main_analysis(oracle.parse_file(params), our_out, threads=2)
+        a, b = our_out.read_bytes(), ref_out.read_bytes()
+        assert len(a) == len(b) and header_equal(a, b), params.read_text()
+        assert a[440:] == b[440:], params.read_text()
