@@ -194,9 +194,14 @@ int st_get_counters(const st_ctx *ctx, st_counters *out);
  * At most 8 parameter sets per call (ST_ERR_ARG beyond).  Every call shares
  * the scratch and it keeps the last call's contents; each call clears what
  * must start at zero, so calls that overlap on the GPU race and must not be
- * issued.  The first call on a device looks the scratch address up with
- * cudaGetSymbolAddress; make it before any stream capture.  Synchronises
- * `stream` (a cudaStream_t, NULL = default stream) before returning. */
+ * issued.  The first call on a device (and the first after its context was
+ * reset) looks the scratch address up with cudaGetSymbolAddress; make it
+ * before any stream capture.  The launch is fixed (the flattened persistent
+ * kernel, 128-thread blocks, as many per SM as fit; no autotuner, no
+ * type-grouped work order): same results as st_run_windows, possibly lower
+ * throughput.  Returns ST_ERR_CUDA when a lane reports that it could not make
+ * progress, as st_run_windows does.  Synchronises `stream` (a cudaStream_t,
+ * NULL = default stream) before returning. */
 int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state_bytes, int w_end, void *stream);
 
 /* ---- discrete adjoint (DOP853 or Magnus CFET8, fixed accepted steps) --- */
@@ -294,7 +299,10 @@ int st_probe_fp64_peak(int device, double *tflops);
 /* The trajectory's correctly rounded libm replacements (log, sin, cos, acos;
  * their results equal the host C library's wherever those are correctly
  * rounded), evaluated over n doubles of a device array x into device array y
- * on the current device, synchronously: fn 0 log, 1 sin, 2 cos, 3 acos.
+ * on the current device, synchronously: fn 0 log, 1 sin, 2 cos, 3 acos,
+ * 4 and 5 sin and cos of acos(x) as a cosine-law reflection takes them;
+ * fn 8-11: the accurate evaluations of log, sin, cos and acos alone (the
+ * fallback the others take when a fast result's rounding is uncertain).
  * For tests; no reference counterpart. */
 int st_crmath_eval(int fn, const double *x, double *y, int64_t n);
 

@@ -47,6 +47,112 @@ void or_set_step_log(double *buf, int64_t cap, int mode) {
 }
 int64_t or_step_log_count(void) { return g_log_n; }
 
+/* ------------------------------------------------------ elementary functions
+ * The trajectory's log, acos, sin and cos: gas clocks -tc log(1 - u)
+ * (src/particle.cpp:117-119), Marsaglia normals sqrt(-2 log s / s) (:89-107)
+ * and cosine-law reflections acos(sqrt u), cos and sin (:309-328).
+ *   mode 0 (default): the host C library, as the reference build calls it;
+ *   mode 1: the correctly rounded double, evaluated in IEEE binary128
+ *     (long double where it is binary128, else __float128 with libquadmath)
+ *     and rounded once.  The binary128 results are within a few units of
+ *     2^-113 relative, so the final rounding errs only where the exact value
+ *     lies that close to a midpoint between doubles (~2^-58 of arguments);
+ *   mode 2: the host C library;
+ *   mode 3: correctly rounded except at one call per particle, the k-th
+ *     (from 0, k per particle from or_set_math_pick) of those whose host
+ *     library result is not the correctly rounded one, which takes the host
+ *     library's result: it isolates the effect of a single last-bit
+ *     difference on a trajectory.
+ * In modes 1-3 each call is audited (or_set_math_audit): per particle the
+ * number of calls whose two results differ and, for the first of them (in
+ * mode 3 the picked one), the particle's time, the function and the
+ * argument.
+ * Test infrastructure for explaining the last-bit differences between the
+ * reference's trajectories and ones computed with correctly rounded
+ * functions; the reference's own results are mode 0. */
+#if defined(__LDBL_MANT_DIG__) && __LDBL_MANT_DIG__ == 113
+typedef long double or_quad;
+#define Q_LOG logl
+#define Q_ACOS acosl
+#define Q_SIN sinl
+#define Q_COS cosl
+#else
+#include <quadmath.h>
+typedef __float128 or_quad;
+#define Q_LOG logq
+#define Q_ACOS acosq
+#define Q_SIN sinq
+#define Q_COS cosq
+#endif
+
+static int g_math_mode = 0;
+static int64_t *g_audit_count = NULL;
+static double *g_audit_t = NULL, *g_audit_arg = NULL;
+static int *g_audit_fn = NULL;
+static int g_audit_n = 0;
+static const int64_t *g_pick = NULL;
+static _Thread_local int tl_part = -1;     /* local slot of the particle being advanced */
+static _Thread_local double tl_time = 0.0; /* its time at the start of the current segment */
+
+void or_set_math_mode(int mode) { g_math_mode = mode; }
+void or_set_math_pick(const int64_t *k) { g_pick = k; }
+void or_set_math_audit(int64_t *count, double *first_t, int *first_fn, double *first_arg, int n) {
+  g_audit_count = count;
+  g_audit_t = first_t;
+  g_audit_fn = first_fn;
+  g_audit_arg = first_arg;
+  g_audit_n = count ? n : 0;
+}
+
+static double cr_eval(int fn, double x) {
+  const or_quad q = (or_quad)x;
+  switch (fn) {
+    case OR_FN_LOG: return (double)Q_LOG(q);
+    case OR_FN_SIN: return (double)Q_SIN(q);
+    case OR_FN_COS: return (double)Q_COS(q);
+    default: return (double)Q_ACOS(q);
+  }
+}
+static double libm_eval(int fn, double x) {
+  switch (fn) {
+    case OR_FN_LOG: return log(x);
+    case OR_FN_SIN: return sin(x);
+    case OR_FN_COS: return cos(x);
+    default: return acos(x);
+  }
+}
+static double tr_fn(int fn, double x) {
+  if (g_math_mode == 0) return libm_eval(fn, x);
+  const double c = cr_eval(fn, x);
+  const double r = libm_eval(fn, x);
+  if (r != c && !(r != r && c != c)) {
+    const int i = tl_part;
+    if (i >= 0 && i < g_audit_n) {
+      const int64_t k = g_audit_count[i]++;
+      const int picked = g_math_mode == 3 && g_pick && g_pick[i] == k;
+      if (k == 0 || picked) { /* mode 3 records the picked call instead of the first */
+        g_audit_t[i] = tl_time;
+        g_audit_fn[i] = fn;
+        g_audit_arg[i] = x;
+      }
+      if (picked) return r;
+    }
+  }
+  return g_math_mode == 2 ? r : c;
+}
+static double tr_log(double x) { return tr_fn(OR_FN_LOG, x); }
+static double tr_acos(double x) { return tr_fn(OR_FN_ACOS, x); }
+static double tr_sin(double x) { return tr_fn(OR_FN_SIN, x); }
+static double tr_cos(double x) { return tr_fn(OR_FN_COS, x); }
+
+void or_math_eval(int fn, int mode, const double *x, double *y, int64_t n, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int64_t k = 0; k < n; ++k) y[k] = mode ? cr_eval(fn, x[k]) : libm_eval(fn, x[k]);
+}
+
 /* ---------------------------------------------------------------- vec3 ops
  * Component-wise restatements of the reference `coords` operators
  * (src/double3.cpp:21-145).  Each returns a new value; order is preserved. */
@@ -262,7 +368,7 @@ double or_normal(or_rng *r, double mean, double std) {
     v = or_uniform_ab(r, -1.0, 1.0);
     s = u * u + v * v;
   } while (s >= 1.0 || s == 0.0);
-  s = sqrt(-2.0 * log(s) / s);
+  s = sqrt(-2.0 * tr_log(s) / s);
   r->spare = v * s;
   r->has_spare = true;
   return mean + std * u * s;
@@ -270,7 +376,7 @@ double or_normal(or_rng *r, double mean, double std) {
 
 static double or_maxboltz(or_rng *r, double sq) { return or_normal(r, 0.0, 1.0) * sq; } /* :109-111 */
 static double or_unif02pi(or_rng *r) { return or_uniform(r) * 2.0 * M_PI; }          /* :113-115 */
-double or_exponential(or_rng *r, double tc) { return -tc * log(1.0 - or_uniform(r)); } /* :117-119 */
+double or_exponential(or_rng *r, double tc) { return -tc * tr_log(1.0 - or_uniform(r)); } /* :117-119 */
 
 /* ------------------------------------------------------------ particles */
 int or_particles_alloc(or_particles *p, int n) {
@@ -295,6 +401,8 @@ void or_particles_free(or_particles *p) {
  * global particle indices first_index.. (the seed uses the global index). */
 void or_init(const or_options *o, or_particles *p, int first_index) {
   for (int i = 0; i < p->n; ++i) {
+    tl_part = i;
+    tl_time = o->t0;
     or_rng r;
     or_rng_seed(&r, o->seed, (unsigned int)(first_index + i));
     or_vec3 pos;
@@ -333,6 +441,7 @@ void or_init(const or_options *o, or_particles *p, int first_index) {
     p->n_coll[i] = 0;
     p->n_steps[i] = 0;
   }
+  tl_part = -1;
 }
 
 /* ------------------------------------------------------------ field model
@@ -961,20 +1070,20 @@ static void advance(const or_options *o, double *t_old, double *t, double dt, or
     if (sz) pos->z = sgn1(pos->z) * o->L.z * 0.5;
     if (o->diffuse > FLT_MIN && or_uniform(rng) < o->diffuse) {
       /* cosine-law diffuse reflection */
-      double phi = acos(sqrt(or_uniform(rng)));
+      double phi = tr_acos(sqrt(or_uniform(rng)));
       double theta = or_unif02pi(rng);
       if (wall_hit == 'x') {
-        v->x = -1 * sgn1(v->x) * speed * cos(phi);
-        v->y = -speed * sin(phi) * cos(theta);
-        v->z = speed * sin(phi) * sin(theta);
+        v->x = -1 * sgn1(v->x) * speed * tr_cos(phi);
+        v->y = -speed * tr_sin(phi) * tr_cos(theta);
+        v->z = speed * tr_sin(phi) * tr_sin(theta);
       } else if (wall_hit == 'y') {
-        v->x = speed * sin(phi) * cos(theta);
-        v->y = -1 * sgn1(v->y) * speed * cos(phi);
-        v->z = speed * sin(phi) * sin(theta);
+        v->x = speed * tr_sin(phi) * tr_cos(theta);
+        v->y = -1 * sgn1(v->y) * speed * tr_cos(phi);
+        v->z = speed * tr_sin(phi) * tr_sin(theta);
       } else if (wall_hit == 'z') {
-        v->x = speed * sin(phi) * cos(theta);
-        v->y = speed * sin(phi) * sin(theta);
-        v->z = -1 * sgn1(v->z) * speed * cos(phi);
+        v->x = speed * tr_sin(phi) * tr_cos(theta);
+        v->y = speed * tr_sin(phi) * tr_sin(theta);
+        v->z = -1 * sgn1(v->z) * speed * tr_cos(phi);
       } else {
         *stop = true; /* diffuse hit on an edge or corner stops the particle */
       }
@@ -1024,6 +1133,8 @@ static void sanity(const or_options *o, double t_old, double t, or_vec3 pos_old,
 
 int or_event(const or_options *o, or_particles *p, int i, double tf) {
   int finished = 0;
+  tl_part = i;
+  tl_time = p->t[i];
   double dt = 0.0;
   next_collision(o, p->t[i], tf, p->v[i], p->pos[i], &p->next_gas[i], &dt, &p->coll_type[i], &p->n_bounce[i],
                  &p->n_coll[i], &finished, &p->wall_hit[i], &p->rng[i]);

@@ -115,6 +115,23 @@ void or_set_counters(or_counters *c);
 void or_set_step_log(double *buf, int64_t cap, int mode);
 int64_t or_step_log_count(void);
 
+/* The trajectory's elementary functions (log, acos, sin, cos): mode 0 the
+ * host C library (the reference's results, default), 1 correctly rounded
+ * (binary128 evaluation, one rounding), 2 the host library, 3 correctly
+ * rounded but for the k-th call per particle whose host result differs
+ * (k from or_set_math_pick; -1 none), which takes the host result.  In modes
+ * 1-3 the audit arrays (n local particle slots, zeroed by the caller) receive
+ * per particle the number of calls whose two results differ and, for the
+ * first (mode 3: the picked one), the particle time at the start of its
+ * segment, the function (OR_FN_*) and the argument; null arrays turn the
+ * audit off. */
+enum { OR_FN_LOG = 0, OR_FN_SIN = 1, OR_FN_COS = 2, OR_FN_ACOS = 3 };
+void or_set_math_mode(int mode);
+void or_set_math_pick(const int64_t *k);
+void or_set_math_audit(int64_t *count, double *first_t, int *first_fn, double *first_arg, int n);
+/* y[k] = fn(x[k]) with the host library (mode 0) or correctly rounded (mode 1). */
+void or_math_eval(int fn, int mode, const double *x, double *y, int64_t n, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

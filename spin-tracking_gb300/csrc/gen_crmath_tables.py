@@ -61,6 +61,22 @@ for name, v in (("kPio2", mp.pi / 2), ("kPio256", mp.pi / 256)):
     p3 = float(rest)
     out.append("constexpr double %s1 = %s, %s2 = %s, %s3 = %s;" % (name, h(p1), name, h(p2), name, h(p3)))
 out.append("constexpr double kTwoOverPi = %s, k256OverPi = %s;" % (h(float(2 / mp.pi)), h(float(256 / mp.pi))))
+# the accurate paths: pi/2 and pi/256 in four parts (33 + 33 + 33 + 53 bits), and the
+# Taylor coefficients 1/n (log1p) and 1/n! (sin, cos) as double-double
+out.append("// Accurate paths: pi/2 and pi/256 in four parts (33 + 33 + 33 + 53 bits).")
+for name, v in (("kPio2q", mp.pi / 2), ("kPio256q", mp.pi / 256)):
+    p1, rest = split(v, 33)
+    p2, rest = split(rest, 33)
+    p3, rest = split(rest, 33)
+    p4 = float(rest)
+    out.append("constexpr double %s1 = %s, %s2 = %s, %s3 = %s, %s4 = %s;" % (name, h(p1), name, h(p2), name, h(p3),
+                                                                         name, h(p4)))
+inv = [(0.0, 0.0)] + [dd(mp.mpf(1) / n) for n in range(1, 24)]
+out.append("// 1/n, n = 0..23 (entry 0 unused), as hi, lo.")
+out.append("static __device__ const double kInvN[24][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in inv) + "};")
+fac = [dd(mp.mpf(1) / mp.factorial(n)) for n in range(0, 20)]
+out.append("// 1/n!, n = 0..19, as hi, lo.")
+out.append("static __device__ const double kInvFact[20][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in fac) + "};")
 # sin, cos of j pi / 256, j = 0..64
 out.append("// sin(j pi / 256), cos(j pi / 256), j = 0..64, as hi, lo.")
 sv = [dd(mp.sin(j * mp.pi / 256)) for j in range(65)]

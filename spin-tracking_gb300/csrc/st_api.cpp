@@ -1353,7 +1353,8 @@ int st_ensemble_stats(st_ctx* c, const void* snap, int set, st_ensemble* out) {
 }
 
 int st_crmath_eval(int fn, const double* x, double* y, int64_t n) {
-  if (fn < 0 || fn > 3 || n < 0 || (n > 0 && (!x || !y))) return fail(ST_ERR_ARG, "st_crmath_eval: bad argument");
+  if (fn < 0 || (fn > 5 && fn < 8) || fn > 11 || n < 0 || (n > 0 && (!x || !y)))
+    return fail(ST_ERR_ARG, "st_crmath_eval: bad argument");
   if (int e = st::launch_crmath_eval(fn, x, y, n, nullptr))
     return fail(ST_ERR_CUDA, std::string("crmath: ") + cudaGetErrorString((cudaError_t)e));
   ST_CUDA(cudaDeviceSynchronize());

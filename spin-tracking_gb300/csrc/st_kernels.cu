@@ -76,11 +76,20 @@ __global__ void k_crmath_eval(int fn, const double* x, double* y, int64_t n) {
   if (i >= n) return;
   const double v = x[i];
   double s, c;
+  if (fn >= 8) {  // the accurate paths alone
+    y[i] = crm::cr_accurate_only(fn - 8, v);
+    return;
+  }
   switch (fn) {
     case 0: y[i] = crm::cr_log(v); break;
     case 1: crm::cr_sincos(v, s, c); y[i] = s; break;
     case 2: crm::cr_sincos(v, s, c); y[i] = c; break;
-    default: y[i] = crm::cr_acos(v); break;
+    case 3: y[i] = crm::cr_acos(v); break;
+    default: {  // the reflection's sin (4) and cos (5) of phi = acos(v), as traj_event takes them
+      double phi;
+      crm::cr_acos_sincos(v, phi, s, c);
+      y[i] = fn == 4 ? s : c;
+    }
   }
 }
 

@@ -18,9 +18,14 @@
 //    call's contents; every call clears the parts that must start at zero
 //    before launching, so calls that overlap on the GPU (different streams or
 //    host threads at once) race on it and must not be issued;
-//  * the first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture.
+//  * the first call on each device (and again after that device's primary
+//    context was reset) looks up the array's device address with
+//    cudaGetSymbolAddress, with that device current; make that first call
+//    before any stream capture;
+//  * the launch is fixed: the flattened persistent kernel (flat_b128_m2)
+//    with as many 128-thread blocks per SM as its occupancy allows, without
+//    the autotuner or the type-grouped work order of st_run_windows (both
+//    allocate); results are the same, throughput can be lower.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,6 +38,7 @@
 namespace st {
 
 constexpr int kNoAllocMaxSets = 8;
+constexpr int kNoAllocVariant = 1;  // flat_b128_m2: flattened persistent kernel, 128 threads, >= 2 blocks per SM
 constexpr size_t kNoAllocScratchBytes = 8192;
 constexpr size_t kNoAllocStatusBytes = 256;  // RunStatus, padded
 static_assert(sizeof(RunStatus) <= kNoAllocStatusBytes, "status block");
@@ -46,19 +52,45 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};  // the context the address was looked up in
+
+// The current driver context (CUcontext), fetched through the runtime's driver
+// entry point so the library does not link libcuda directly.  A primary
+// context that was reset (cudaDeviceReset) comes back as a new context, in
+// which the module is loaded again and the array may sit at another address.
+typedef int (*CtxGetCurrentFn)(void**);
+void* current_context() {
+  static CtxGetCurrentFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(f);
+  }();
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 // Device address of the scratch array on the current device.  In host code the
-// array's name is only a stand-in for the symbol, never a usable pointer.
+// array's name is only a stand-in for the symbol, never a usable pointer.  The
+// address is looked up once per device and context; before the runtime's first
+// call on a device no context is current yet, and the lookup itself makes the
+// primary context current.
 int scratch_address(int device, unsigned char** out) {
   if (device < 0 || device >= kMaxDevices) return set_last_error(ST_ERR_ARG, "device index out of range");
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[device]) {
+  void* ctx = current_context();
+  if (!g_scratch_addr[device] || !ctx || ctx != g_scratch_ctx[device]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       return set_last_error(ST_ERR_CUDA, (std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e)).c_str());
     }
     g_scratch_addr[device] = p;
+    // the runtime has made the primary context current by now
+    g_scratch_ctx[device] = ctx ? ctx : current_context();
   }
   *out = static_cast<unsigned char*>(g_scratch_addr[device]);
   return ST_OK;
@@ -176,14 +208,21 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
     k_noalloc_sets<<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(a.s, params, nsets);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_last_error(ST_ERR_CUDA, cudaGetErrorString(e));
+    // flat_b128_m2 (the flattened persistent kernel) at its full occupancy; the
+    // occupancy query and the shared-memory attribute allocate nothing
+    const int per_sm = persistent_max_blocks_per_sm(kNoAllocVariant, a.any_ext);
+    if (per_sm < 1) return set_last_error(ST_ERR_CUDA, "st_run_noalloc: the persistent kernel cannot be resident");
     int le = launch_init(a, 256, st_);
-    if (!le) le = launch_persistent(a, 1, sms, 0, st_);  // variant b128_m2, one block per SM
+    if (!le) le = launch_persistent(a, kNoAllocVariant, sms * per_sm, 0, st_);
     if (le) return set_last_error(ST_ERR_CUDA, cudaGetErrorString((cudaError_t)le));
   }
   RunStatus h{};
   e = cudaMemcpyAsync(&h, status, sizeof(RunStatus), cudaMemcpyDeviceToHost, st_);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
-  if (e != cudaSuccess) return set_last_error(ST_ERR_CUDA, cudaGetErrorString(e));
+  if (e != cudaSuccess) return set_last_error(ST_ERR_CUDA, (std::string("kernel execution: ") + cudaGetErrorString(e)).c_str());
   *state_bytes_io = need;
+  // the same status checks as the allocating path's run end
+  if (h.pad) return set_last_error(ST_ERR_CUDA, "internal: a persistent-kernel lane could not make progress");
+  if (h.deadline_hit) return set_last_error(ST_ERR_DEADLINE, "device time budget ran out");
   return ST_OK;
 }

@@ -75,6 +75,10 @@ class Oracle:
             "or_set_counters": (None, [c_void_p]),
             "or_set_step_log": (None, [c_void_p, ctypes.c_int64, c_int]),
             "or_step_log_count": (ctypes.c_int64, []),
+            "or_set_math_mode": (None, [c_int]),
+            "or_set_math_pick": (None, [c_void_p]),
+            "or_set_math_audit": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
+            "or_math_eval": (None, [c_int, c_int, c_void_p, c_void_p, ctypes.c_int64, c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -82,6 +86,66 @@ class Oracle:
             f.argtypes = args
         self.L = L
         assert L.or_options_size() == 440
+
+    # elementary functions of the trajectory ------------------------------
+    MATH_LIBM, MATH_CR, MATH_AUDIT, MATH_PICK = 0, 1, 2, 3
+    FN = {"log": 0, "sin": 1, "cos": 2, "acos": 3}
+    FN_NAMES = {v: k for k, v in FN.items()}
+
+    def math_eval(self, fn: str, x, correctly_rounded: bool, threads: int = 0):
+        """fn(x) elementwise: the host C library, or correctly rounded
+        (binary128 evaluation rounded once)."""
+        import numpy as np
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        self.L.or_math_eval(self.FN[fn], 1 if correctly_rounded else 0, x.ctypes.data, y.ctypes.data, x.size,
+                            threads)
+        return y
+
+    def set_math_mode(self, mode: int) -> None:
+        self.L.or_set_math_mode(mode)
+
+    def run_sample_audited(self, opt: Options, first: int, count: int, threads: int = 0, mode: int = 2,
+                           snapshots: bool = False, pick=None):
+        """run_sample with the trajectory's elementary functions in `mode`
+        (MATH_AUDIT: the host library; MATH_CR: correctly rounded; MATH_PICK:
+        correctly rounded but for the pick[i]-th call of particle i whose
+        host result differs), each call audited against the other result.
+        Returns (seconds, arrays, audit) where audit holds per particle the
+        number of calls whose host result was not correctly rounded and, for
+        the first, the particle time at the start of its segment, the function
+        and the argument.  With snapshots=True the arrays are a list over the
+        snapshots t0, t0 + ioutInt, ...; the math mode is restored to the host
+        library on return."""
+        import numpy as np
+        cnt = np.zeros(count, np.int64)
+        t1 = np.full(count, np.inf)
+        fn = np.full(count, -1, np.int32)
+        arg = np.full(count, np.nan)
+        pk = np.ascontiguousarray(pick if pick is not None else np.full(count, -1), dtype=np.int64)
+        self.L.or_set_math_pick(pk.ctypes.data)
+        self.L.or_set_math_mode(mode)
+        self.L.or_set_math_audit(cnt.ctypes.data, t1.ctypes.data, fn.ctypes.data, arg.ctypes.data, count)
+        p = self.alloc(count)
+        try:
+            if snapshots:
+                nwin = int(np.floor((opt.tf - opt.t0) / opt.ioutInt))
+                t0 = __import__("time").perf_counter()
+                self.L.or_init(ctypes.byref(opt), ctypes.byref(p), first)
+                out = [self.arrays(p)]
+                for w in range(nwin):
+                    self.L.or_run_until(ctypes.byref(opt), ctypes.byref(p), (w + 1.0) * opt.ioutInt, threads)
+                    out.append(self.arrays(p))
+                secs = __import__("time").perf_counter() - t0
+            else:
+                secs = self.L.or_run_sample(ctypes.byref(opt), first, count, threads, ctypes.byref(p))
+                out = self.arrays(p)
+        finally:
+            self.free(p)
+            self.L.or_set_math_audit(None, None, None, None, 0)
+            self.L.or_set_math_pick(None)
+            self.L.or_set_math_mode(self.MATH_LIBM)
+        return secs, out, {"count": cnt, "first_t": t1, "first_fn": fn, "first_arg": arg}
 
     # options -------------------------------------------------------------
     def default_options(self) -> Options:

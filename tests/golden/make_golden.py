@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ by running the REFERENCE build.
 
-Requires the reference sources (default /root/reference, or $SPINTRACK_REF)
+Requires the reference sources (the oracle recipe's REF, or $SPINTRACK_REF)
 and builds them with `make -C oracle ref` (the reference's own .cpp files
 compiled unchanged against oracle/ref_stubs).  Writes, per case:
   <case>.params          the params.txt the reference read
@@ -21,7 +21,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 ORACLE = REPO / "oracle"
-REF = Path(os.environ.get("SPINTRACK_REF", "/root/reference"))
+# where the reference sources are: $SPINTRACK_REF, else the oracle recipe's default
+REF_ARGS = [f"REF={os.environ['SPINTRACK_REF']}"] if os.environ.get("SPINTRACK_REF") else []
 
 BASE = {
     "L": "0.07, 0.1, 0.4", "B0": "3e-6, 0, 0", "E": "0, 0, 75e5", "gamma": "-2.038e8", "m": "1.20239e-26",
@@ -112,10 +113,7 @@ def run(cmd, **kw):
 
 
 def main() -> int:
-    if not (REF / "src" / "particle.cpp").exists():
-        print(f"reference sources not found at {REF}", file=sys.stderr)
-        return 1
-    r = run(["make", "-C", str(ORACLE), "ref", f"REF={REF}"])
+    r = run(["make", "-C", str(ORACLE), "ref", *REF_ARGS])
     if r.returncode:
         print(r.stdout, r.stderr, file=sys.stderr)
         return 1
