@@ -99,12 +99,14 @@ __device__ __forceinline__ bool rounds_surely(double hi, double lo, double err) 
 }
 
 // Error bounds, relative to the result (and absolute, from the argument
-// reduction of sin and cos): fast paths conservatively above their analysed
-// errors (log ~2^-74, sin/cos ~2^-66, acos ~2^-66), accurate paths above ~2^-100.
-constexpr double kLogFastErr = 0x1p-68;
-constexpr double kTrigFastErr = 0x1p-63, kTrigAbsErr = 0x1p-112;
-constexpr double kAcosFastErr = 0x1p-62;
-constexpr double kAccurateErr = 0x1p-96;
+// reduction of sin and cos), set above the largest errors measured against
+// binary128 on 5 10^6 trajectory arguments per function (log 2^-74.6,
+// sin/cos 2^-83.4, acos 2^-84.0): a fast result is kept only when no rounding
+// boundary lies within the bound, which sends about 2^-17 (log) and 2^-24
+// (sin, cos, acos) of the calls to the accurate paths.
+constexpr double kLogFastErr = 0x1p-71;
+constexpr double kTrigFastErr = 0x1p-78, kTrigAbsErr = 0x1p-112;
+constexpr double kAcosFastErr = 0x1p-78;
 __device__ __forceinline__ double rel_err(double v, double rel) { return __dmul_ru(fabs(v), rel); }
 
 // ---------------------------------------------------------------- log
@@ -180,7 +182,7 @@ static __device__ __noinline__ double cr_log(double x) {
 
 // ---------------------------------------------------------------- sin, cos
 // sin and cos of x, 0 <= |x| < 2^20, as double-double values accurate to
-// ~2^-67 relative.
+// ~2^-83 relative (absolute ~2^-120 from the reduction).
 __device__ __forceinline__ void sincos_dd(double x, DD& sn, DD& cs) {
   // x = k pi/2 + r, r as double-double (k * kPio21 and k * kPio22 are exact)
   const double k = rint(__dmul_rn(x, kTwoOverPi));
@@ -192,12 +194,25 @@ __device__ __forceinline__ void sincos_dd(double x, DD& sn, DD& cs) {
   DD s = two_sum(__fma_rn(-jd, kPio2561, r.hi), __dmul_rn(-jd, kPio2562));
   s = dd_add_d(s, r.lo);
   const double sh = s.hi, sl = __fma_rn(-jd, kPio2563, s.lo);
-  // sin s - s and cos s - 1 by their Taylor series in double (to s^7 and s^6)
-  const double z = __dmul_rn(sh, sh);
-  const double sp = __dmul_rn(__dmul_rn(sh, z), __fma_rn(z, __fma_rn(z, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0));
-  const double cp = __fma_rn(-sh, sl, __dmul_rn(z, __fma_rn(z, __fma_rn(z, -1.0 / 720.0, 1.0 / 24.0), -0.5)));
-  // angle addition with the table at a = j pi / 256: the leading products
-  // exact, the small terms in double
+  // s = sh + sl.  z = sh^2 exactly.  sin s = sh + sl + p3 + p5 with
+  // p3 = -s^3 / 6 in double-double (s^3 = sh z.hi exactly plus sh z.lo +
+  // 3 z.hi sl) and p5 = s^5 / 5! - s^7 / 7! + s^9 / 9! in double;
+  // cos s - 1 = cph + cpl with cph = -z.hi / 2 exact and cpl = -z.lo / 2 -
+  // sh sl + s^4 / 4! - s^6 / 6! + s^8 / 8!.
+  const DD z = two_prod(sh, sh);
+  DD s3 = two_prod(sh, z.hi);
+  s3.lo = __fma_rn(3.0 * z.hi, sl, __fma_rn(sh, z.lo, s3.lo));
+  const DD p3 = dd_mul(s3, {-kSixthHi, -kSixthLo});
+  const double p5 = __dmul_rn(__dmul_rn(s3.hi, z.hi),
+                             __fma_rn(z.hi, __fma_rn(z.hi, 1.0 / 362880.0, -1.0 / 5040.0), 1.0 / 120.0));
+  const double cph = __dmul_rn(-0.5, z.hi);
+  const double cpl = __fma_rn(__dmul_rn(z.hi, z.hi),
+                              __fma_rn(z.hi, __fma_rn(z.hi, 1.0 / 40320.0, -1.0 / 720.0), 1.0 / 24.0),
+                              __fma_rn(-sh, sl, __dmul_rn(-0.5, z.lo)));
+  // angle addition with the table at a = j pi / 256: the leading terms (the
+  // table value, cos a sh, sin a cph and cos a p3.hi for sin; their
+  // counterparts for cos) summed exactly, the rest (below 2^-34 of the
+  // result) in double
   const int ja = (int)fabs(jd);
   double sah = kSinA[ja][0], sal = kSinA[ja][1];
   if (jd < 0.0) {
@@ -205,19 +220,20 @@ __device__ __forceinline__ void sincos_dd(double x, DD& sn, DD& cs) {
     sal = -sal;
   }
   const double cah = kCosA[ja][0], cal = kCosA[ja][1];
-  const double ss = __dadd_rn(sl, sp);  // sin s - sh
-  // sin(a + s) = sin a + cos a sh + [cos a (sin s - sh) + sin a (cos s - 1)]
-  const DD m = two_prod(cah, sh);
-  const DD hs = two_sum(sah, m.hi);
-  const double ts = __dadd_rn(__dadd_rn(m.lo, sal),
-                              __fma_rn(cal, sh, __fma_rn(sah, cp, __dmul_rn(cah, ss))));
-  const DD sr = fast_two_sum(hs.hi, __dadd_rn(hs.lo, ts));
-  // cos(a + s) = cos a - sin a sh + [cos a (cos s - 1) - sin a (sin s - sh)]
-  const DD m2 = two_prod(-sah, sh);
-  const DD hc = two_sum(cah, m2.hi);
-  const double tc = __dadd_rn(__dadd_rn(m2.lo, cal),
-                              __fma_rn(-sal, sh, __fma_rn(cah, cp, __dmul_rn(-sah, ss))));
-  const DD cr = fast_two_sum(hc.hi, __dadd_rn(hc.lo, tc));
+  const double rest_s = __dadd_rn(__dadd_rn(sl, p3.lo), p5);  // sin s - sh - p3.hi
+  // sin(a + s) = sin a + cos a (sin s) + sin a (cos s - 1)
+  const DD e1 = two_prod(cah, sh), e2 = two_prod(sah, cph), e3 = two_prod(cah, p3.hi);
+  const DD h1 = two_sum(sah, e1.hi), h2 = two_sum(h1.hi, e2.hi), h3 = two_sum(h2.hi, e3.hi);
+  const double sh3 = __dadd_rn(sh, p3.hi);  // the low table parts multiply sin s to 2^-60
+  double ts = __fma_rn(cah, rest_s, __fma_rn(cal, sh3, __fma_rn(sah, cpl, __fma_rn(sal, cph, sal))));
+  ts = __dadd_rn(ts, __dadd_rn(__dadd_rn(__dadd_rn(e1.lo, e2.lo), e3.lo), __dadd_rn(__dadd_rn(h1.lo, h2.lo), h3.lo)));
+  const DD sr = fast_two_sum(h3.hi, ts);
+  // cos(a + s) = cos a - sin a (sin s) + cos a (cos s - 1)
+  const DD f1 = two_prod(-sah, sh), f2 = two_prod(cah, cph), f3 = two_prod(-sah, p3.hi);
+  const DD g1 = two_sum(cah, f1.hi), g2 = two_sum(g1.hi, f2.hi), g3 = two_sum(g2.hi, f3.hi);
+  double tc = __fma_rn(-sah, rest_s, __fma_rn(-sal, sh3, __fma_rn(cah, cpl, __fma_rn(cal, cph, cal))));
+  tc = __dadd_rn(tc, __dadd_rn(__dadd_rn(__dadd_rn(f1.lo, f2.lo), f3.lo), __dadd_rn(__dadd_rn(g1.lo, g2.lo), g3.lo)));
+  const DD cr = fast_two_sum(g3.hi, tc);
   // quadrant
   const int q = ((int)k) & 3;
   if (q == 0) {
