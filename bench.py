@@ -464,6 +464,7 @@ def run_workload(args):
                  "tape_gb": stats["tape_bytes_used"] / 1e9, "pool_gb": stats["tape_bytes_pool"] / 1e9,
                  "tape_resident": bool(stats["resident"]), "checkpoints": stats["checkpoints"],
                  "replays_per_backward": bstats["replays"], "groups_per_backward": bstats["groups"],
+                 "tail_from_checkpoint": stats["tail_from"], "record_launches": stats["record_launches"],
                  "backward_all_losses_one_call_s": t_multi})
     if pulse:
         g = grads["P"]
@@ -477,6 +478,14 @@ def run_workload(args):
 
 
 # ---------------------------------------------------------------- main
+def workload_config(args, world):
+    """The `config` object of both arms' lines: the workload and its sizes."""
+    sim = int(args.tf / 0.5) * 0.5
+    return {"workload": WORKLOAD, "particles": args.particles, "tf": sim, "windows": int(args.tf / 0.5),
+            "l2": "inputs larger than L2: per-particle state 178 MB + snapshot blocks, rewritten each step",
+            "parallelism": f"particle shards x{world}"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
@@ -488,11 +497,14 @@ def run_reference(args, world, rank):
         if i >= args.warmup:
             rates.append(r)
     v = statistics.mean(rates)
-    sim = int(args.tf / 0.5) * 0.5
+    # the same workload keys as the repo arm's line; the CPU times a bounded
+    # sample of it each step (particles are independent and seeded by their
+    # global index, so the rate of a sample is the rate of the workload)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "particles_per_step": "bounded sample", "tf": sim},
+            "config": workload_config(args, 1),
+            "sample_per_step": sample,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -533,6 +545,7 @@ def run_ours(args, world, rank, local):
         step()
     counters = p.counters()
     lcfg = p.launch_config()
+    lcfg_name = st.variant_name(lcfg[0]) if lcfg[0] >= 0 else None
 
     # ---- timed region: K steps, CUDA events on the launching stream
     torch.cuda.synchronize()
@@ -634,10 +647,9 @@ def run_ours(args, world, rank, local):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "particles": n_total, "tf": sim, "windows": nwin,
-                           "kernel": args.kernel, "launch_config": {"variant": lcfg[0], "blocks_per_sm": lcfg[1]},
-                           "l2": "inputs larger than L2: per-particle state 178 MB + snapshot blocks, rewritten each step",
-                           "parallelism": f"particle shards x{world}"},
+                "config": workload_config(args, world),
+                "kernel": args.kernel,
+                "launch_config": {"variant": lcfg[0], "name": lcfg_name, "blocks_per_sm": lcfg[1]},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain_kernel": plain, "adjoint": adjoint,
                 "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line), flush=True)

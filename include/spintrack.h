@@ -214,12 +214,15 @@ int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state
  * st_run_windows does (the trajectory-ahead kernel), and writes the adjoint's
  * tape: every accepted step (y, x, h) and every integrated segment
  * (t0, p0, v0) of every particle, in pages of a device pool of tape_bytes
- * (0 = up to 45% of free device memory).  It also keeps a full-state
+ * (0 = up to 75% of free device memory).  It also keeps a full-state
  * checkpoint every windows_per_checkpoint windows (0 = chosen so the
- * checkpoints take at most 10% of free memory).  When the tape does not fit
- * the pool, st_adjoint_backward replays window chunks from the checkpoints
- * (and, if one window's tape does not fit, groups of particles), so results
- * do not depend on the pool size.  All sets of the context integrate with
+ * checkpoints take at most 10% of free memory).  A run of four or more
+ * checkpoint intervals is recorded in pieces: the first interval's tape
+ * projects the whole tape; when that does not fit the pool, only the last
+ * intervals that fit are stored (the rest of the run keeps checkpoints only)
+ * and st_adjoint_backward takes them first, then replays window chunks of the
+ * earlier intervals from the checkpoints (and, if one window's tape does not
+ * fit, groups of particles), so results do not depend on the pool size.  All sets of the context integrate with
  * DOP853 (integratorType 0) or all with Magnus CFET8 (2); the linear grad
  * hook only.
  * No counterpart in the reference (it has no derivatives). */
@@ -244,6 +247,10 @@ typedef struct {
   int32_t windows_per_checkpoint;
   int32_t replays;            /* replay launches of the last backward */
   int32_t groups;             /* particle-group replays among them */
+  int32_t tail_from;          /* when the whole tape did not fit: the checkpoint interval from which the record
+                                 pass kept it (the backward replays only the intervals before); = checkpoints
+                                 when nothing was kept apart */
+  int32_t record_launches;    /* kernel launches of the record pass */
   int32_t pad;
 } st_adjoint_stats;
 int st_adjoint_get_stats(const st_ctx *ctx, st_adjoint_stats *out);

@@ -81,20 +81,33 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
     ST_OS(s, 2) = O[2];
     if (s < 12) bloch(Y[0], Y[1], Y[2], O[0], O[1], O[2], K[s - 1][0], K[s - 1][1], K[s - 1][2]);
   }
-  // ---- backward sweep, stage 12 first
-  double kh[12][3];
-#pragma unroll
-  for (int s = 1; s <= 12; ++s)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) kh[s - 1][c] = (dopst::b(s) != 0.0) ? dopst::b(s) * lam[c] : 0.0;
+  // ---- backward sweep, stage 12 first.  kh_s is gathered when stage s is
+  // reached, from the yb_r of the later stages (r = 12 first, the order in
+  // which they are produced), which replace their stage states in shared
+  // memory once read: no array of twelve accumulators stays live.
+  const double lam0[3] = {lam[0], lam[1], lam[2]};
 #pragma unroll
   for (int s = 12; s >= 1; --s) {
-    const double kb[3] = {h * kh[s - 1][0], h * kh[s - 1][1], h * kh[s - 1][2]};
+    double kb[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double acc = (dopst::b(s) != 0.0) ? dopst::b(s) * lam0[c] : 0.0;
+#pragma unroll
+      for (int r = 12; r > s; --r) {
+#pragma unroll
+        for (int j = 0; j < dopst::cnt(r); ++j)
+          if (dopst::src(r, j) == s) acc = fma(dopst::a(r, j), ST_YS(r, c), acc);
+      }
+      kb[c] = h * acc;
+    }
     const double O[3] = {ST_OS(s, 0), ST_OS(s, 1), ST_OS(s, 2)};
     const double Y[3] = {ST_YS(s, 0), ST_YS(s, 1), ST_YS(s, 2)};
     double yb[3], z[3];
     cross3(O, kb, yb);  // dL/dY_s
     cross3(kb, Y, z);   // dL/dOmega_s
+    ST_YS(s, 0) = yb[0];
+    ST_YS(s, 1) = yb[1];
+    ST_YS(s, 2) = yb[2];
     const double tau = stage_tau(s, tx, h);
     const double tau2 = tau * tau;
 #pragma unroll
@@ -110,12 +123,6 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
       sincos(P.w * t, &sn, &cs);
       M.ga = fma(P.gamma * cs, z[2], M.ga);
       M.gw = fma(-P.gamma * P.a * t * sn, z[2], M.gw);
-    }
-#pragma unroll
-    for (int j = 0; j < dopst::cnt(s); ++j) {
-      const int l = dopst::src(s, j) - 1;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) kh[l][c] = fma(dopst::a(s, j), yb[c], kh[l][c]);
     }
   }
 #undef ST_YS

@@ -187,7 +187,11 @@ struct st_ctx {
   void* tape_pp = nullptr;   // per-particle tape arrays and work orders
   unsigned long long* tape_head = nullptr;
   long long* tape_error = nullptr;
-  st::TapeArgs tape{};       // pointers into the above
+  st::TapeArgs tape{};       // pointers into the above: the chains of replays (and of a record whose tape fits)
+  st::TapeArgs tail{};       // the chains of the record pass's last intervals (kept when the whole tape does not fit)
+  unsigned long long* tail_head = nullptr;
+  int adj_tail_from = 0;          // checkpoint interval where the kept tail starts (ckpt_count: no tail)
+  int64_t adj_tail_pages = 0;     // pool pages the record pass's tape holds (replays use the pages after them)
   int64_t* adj_order = nullptr;   // every particle, longest tape first
   int64_t* adj_gorder = nullptr;  // a group of particles replayed together
   void* ckpt_arena = nullptr;     // state checkpoints, ckpt_count arenas
@@ -622,6 +626,7 @@ void st_destroy(st_ctx* c) {
   cudaFree(c->tape_prev);
   cudaFree(c->tape_pp);
   cudaFree(c->tape_head);
+  cudaFree(c->tail_head);
   cudaFree(c->tape_error);
   cudaFree(c->ckpt_arena);
   cudaFree(c->replay_arena);
@@ -899,6 +904,8 @@ namespace {
 constexpr size_t kPageBytes = sizeof(double) * st::kTapePageD;
 
 // Pages a particle's tape needs for n steps and m segments.
+int64_t adj_replay_pages(const st_ctx* c);
+
 inline int64_t tape_pages_for(int64_t steps, int64_t segs) {
   return (steps + st::kTapeStepsPerPage - 1) / st::kTapeStepsPerPage +
          (segs + st::kTapeSegsPerPage - 1) / st::kTapeSegsPerPage;
@@ -908,38 +915,42 @@ inline int64_t tape_pages_for(int64_t steps, int64_t segs) {
 int adj_alloc_particle_arrays(st_ctx* c) {
   if (c->tape_pp) return ST_OK;
   const size_t m = (size_t)std::max<int64_t>(c->n, 1);
-  const size_t sz[] = {4 * m, 4 * m, 4 * m, 4 * m, 4 * m, 8 * m, 8 * m, 8 * m, 8 * m};
-  size_t total = 0;
-  for (size_t x : sz) total += align256(x);
+  // two chain sets (replays, record) of 7 arrays, then the two work orders
+  const size_t chain[] = {4 * m, 4 * m, 4 * m, 4 * m, 4 * m, 8 * m, 8 * m};
+  size_t total = 2 * align256(8 * m);
+  for (size_t x : chain) total += 2 * align256(x);
   cudaError_t e = cudaMalloc(&c->tape_pp, total);
   if (e != cudaSuccess) return fail(ST_ERR_NOMEM, std::string("adjoint arrays: ") + cudaGetErrorString(e));
   char* p = (char*)c->tape_pp;
-  void* ptr[9];
-  for (int k = 0; k < 9; ++k) {
-    ptr[k] = p;
-    p += align256(sz[k]);
+  auto take = [&](size_t bytes) {
+    void* q = p;
+    p += align256(bytes);
+    return q;
+  };
+  for (st::TapeArgs* t : {&c->tape, &c->tail}) {
+    t->step_page = (int32_t*)take(chain[0]);
+    t->step_fill = (int32_t*)take(chain[1]);
+    t->seg_page = (int32_t*)take(chain[2]);
+    t->seg_fill = (int32_t*)take(chain[3]);
+    t->complete = (int32_t*)take(chain[4]);
+    t->nsteps = (int64_t*)take(chain[5]);
+    t->nsegs = (int64_t*)take(chain[6]);
   }
-  st::TapeArgs& t = c->tape;
-  t.step_page = (int32_t*)ptr[0];
-  t.step_fill = (int32_t*)ptr[1];
-  t.seg_page = (int32_t*)ptr[2];
-  t.seg_fill = (int32_t*)ptr[3];
-  t.complete = (int32_t*)ptr[4];
-  t.nsteps = (int64_t*)ptr[5];
-  t.nsegs = (int64_t*)ptr[6];
-  c->adj_order = (int64_t*)ptr[7];
-  c->adj_gorder = (int64_t*)ptr[8];
+  c->adj_order = (int64_t*)take(8 * m);
+  c->adj_gorder = (int64_t*)take(8 * m);
   ST_CUDA(cudaMalloc(&c->tape_head, sizeof(unsigned long long)));
+  ST_CUDA(cudaMalloc(&c->tail_head, sizeof(unsigned long long)));
   ST_CUDA(cudaMalloc(&c->tape_error, sizeof(long long) * st::kTapeErrorSlots));
-  t.pool_head = c->tape_head;
-  t.error = c->tape_error;
+  c->tape.pool_head = c->tape_head;
+  c->tail.pool_head = c->tail_head;
+  c->tape.error = c->tail.error = c->tape_error;
   return ST_OK;
 }
 
-// Clear the per-particle chain heads and the pool cursor before a tape pass.
-int adj_reset_tape(st_ctx* c) {
+// Clear the per-particle chain heads and the pool cursor of a chain set
+// (c->tape: replays; c->tail: the record pass) before a tape pass.
+int adj_reset_tape(st_ctx* c, const st::TapeArgs& t) {
   const size_t m = (size_t)std::max<int64_t>(c->n, 1);
-  st::TapeArgs& t = c->tape;
   ST_CUDA(cudaMemsetAsync(t.step_page, 0xff, 4 * m, c->stream));
   ST_CUDA(cudaMemsetAsync(t.seg_page, 0xff, 4 * m, c->stream));
   ST_CUDA(cudaMemsetAsync(t.step_fill, 0, 4 * m, c->stream));
@@ -947,10 +958,11 @@ int adj_reset_tape(st_ctx* c) {
   ST_CUDA(cudaMemsetAsync(t.complete, 0, 4 * m, c->stream));
   ST_CUDA(cudaMemsetAsync(t.nsteps, 0, 8 * m, c->stream));
   ST_CUDA(cudaMemsetAsync(t.nsegs, 0, 8 * m, c->stream));
-  ST_CUDA(cudaMemsetAsync(c->tape_head, 0, sizeof(unsigned long long), c->stream));
+  ST_CUDA(cudaMemsetAsync(t.pool_head, 0, sizeof(unsigned long long), c->stream));
   ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(long long) * st::kTapeErrorSlots, c->stream));
   return ST_OK;
 }
+int adj_reset_replay_tape(st_ctx* c) { return adj_reset_tape(c, c->tape); }
 
 int adj_tape_launch(st_ctx* c, const st::RunArgs& a, const st::TapeArgs& t) {
   const int per_sm = std::max(1, st::tape_record_max_blocks_per_sm(ctx_any_ext(c) ? 1 : 0));
@@ -1024,7 +1036,7 @@ int adj_replay_and_back(st_ctx* c, int slot, int b_hi, const std::vector<int64_t
   if (group) ST_TRY(adj_upload_order(c, *group, c->adj_gorder));
   ST_CUDA(cudaMemcpyAsync(c->replay_arena, (char*)c->ckpt_arena + (size_t)slot * c->arena_bytes, c->arena_bytes,
                           cudaMemcpyDeviceToDevice, c->stream));
-  ST_TRY(adj_reset_tape(c));
+  ST_TRY(adj_reset_replay_tape(c));
   ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
   st::RunArgs a = make_args(c, 0, b_hi, nullptr);
   a.s = adj_view(c, c->replay_arena);
@@ -1090,26 +1102,53 @@ int adj_chunk(st_ctx* c, int k_lo, int k_hi, const st::TapeArgs& tb) {
   for (size_t i = 0; i < n; ++i) {
     if (c->adj_stop_h[i]) continue;
     const int64_t need = tape_pages_for(ns[i], ng[i]);
-    if (need > c->tape_pages)
+    if (need > adj_replay_pages(c))
       return fail(ST_ERR_NOMEM, "one particle's tape over one checkpoint interval is larger than the tape pool: "
                                 "raise tape_bytes or lower windows_per_checkpoint");
-    if (used + need > c->tape_pages) ST_TRY(flush());
+    if (used + need > adj_replay_pages(c)) ST_TRY(flush());
     group.push_back((int64_t)i);
     used += need;
   }
   return flush();
 }
 
-st::TapeArgs adj_tape_args(st_ctx* c) {
-  st::TapeArgs t = c->tape;
-  t.pool = c->tape_pool;
-  t.page_prev = c->tape_prev;
-  t.pool_pages = c->tape_pages;
+// Tape arguments over pool pages [first, first + pages) with chain set `chains`.
+st::TapeArgs adj_region(st_ctx* c, const st::TapeArgs& chains, int64_t first, int64_t pages) {
+  st::TapeArgs t = chains;
+  t.pool = c->tape_pool + (size_t)first * st::kTapePageD;
+  t.page_prev = c->tape_prev + first;
+  t.pool_pages = pages;
+  t.append = 0;
   t.ckpt = adj_view(c, c->ckpt_arena);
   t.ckpt_stride = (int64_t)c->arena_bytes;
   t.ckpt_every = c->ckpt_every;
   t.ckpt_count = c->ckpt_count;
   return t;
+}
+// Replays: the pages after the record pass's own tape.
+int64_t adj_replay_pages(const st_ctx* c) { return c->tape_pages - c->adj_tail_pages; }
+st::TapeArgs adj_tape_args(st_ctx* c) { return adj_region(c, c->tape, c->adj_tail_pages, adj_replay_pages(c)); }
+// The record pass's own tape (all of it when it fits, else its last intervals).
+st::TapeArgs adj_record_args(st_ctx* c, int64_t pages) { return adj_region(c, c->tail, 0, pages); }
+
+// One record launch up to window w_hi (the particles continue from their own
+// window counters); the chains' counts are added to the totals (an appending
+// launch continues the counts it was given).
+int adj_record_launch(st_ctx* c, int w_hi, const st::TapeArgs& t, std::vector<int64_t>& ns_tot,
+                      std::vector<int64_t>& ng_tot) {
+  ST_TRY(begin_run(c));
+  st::RunArgs a = make_args(c, 0, w_hi, nullptr);
+  ST_TRY(adj_tape_launch(c, a, t));
+  const size_t n = (size_t)c->n;
+  std::vector<int64_t> ns(std::max<size_t>(n, 1)), ng(std::max<size_t>(n, 1));
+  ST_CUDA(cudaMemcpyAsync(ns.data(), t.nsteps, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaMemcpyAsync(ng.data(), t.nsegs, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_TRY(end_run(c, 1));
+  for (size_t i = 0; i < n; ++i) {
+    ns_tot[i] = t.append ? ns[i] : ns_tot[i] + ns[i];
+    ng_tot[i] = t.append ? ng[i] : ng_tot[i] + ng[i];
+  }
+  return ST_OK;
 }
 
 }  // namespace
@@ -1160,7 +1199,7 @@ int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_c
   size_t want = tape_bytes;
   if (want == 0) {
     ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const double cap = 0.45 * (double)free_b;
+    const double cap = 0.75 * (double)free_b;
     const double guess = (double)std::max<int64_t>(c->n, 1) * 16.0 * 1048576.0 + 64.0 * 1048576.0;
     want = (size_t)std::min(cap, guess);
   }
@@ -1183,29 +1222,79 @@ int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_c
     const st::DeviceState v = adj_view(c, (char*)c->ckpt_arena + (size_t)k * c->arena_bytes);
     ST_CUDA(cudaMemsetAsync(v.w_done, 0x7f, 4 * (size_t)std::max<int64_t>(c->n, 1), c->stream));
   }
-  ST_TRY(adj_reset_tape(c));
-  ST_TRY(begin_run(c));
-  st::RunArgs a = make_args(c, 0, w_end, nullptr);
-  const st::TapeArgs t = adj_tape_args(c);
-  ST_TRY(adj_tape_launch(c, a, t));
+  // The record pass stores its tape with its own chain set from pool page 0.
+  // A run of four or more checkpoint intervals is recorded in pieces: the
+  // first interval with the tape on, whose length projects the whole tape
+  // (time-uniform); if that fits the pool, the rest continues the same chains;
+  // if not, the middle runs with the tape off (state checkpoints only) and the
+  // last intervals that fit -- the ones the backward needs first -- are stored
+  // afresh, leaving the pages after them for the backward's replays.
   const size_t n = (size_t)c->n;
   c->adj_nsteps_h.assign(std::max<size_t>(n, 1), 0);
   c->adj_nsegs_h.assign(std::max<size_t>(n, 1), 0);
   c->adj_stop_h.assign(std::max<size_t>(n, 1), 0);
+  c->adj_tail_from = count;
+  c->adj_tail_pages = 0;
+  st::TapeArgs t = adj_record_args(c, c->tape_pages);
+  ST_TRY(adj_reset_tape(c, t));
+  int launches = 0;
+  bool tail_mode = false;
+  if (count >= 4 && w_run > every) {
+    ST_TRY(adj_record_launch(c, every, t, c->adj_nsteps_h, c->adj_nsegs_h));
+    ++launches;
+    int64_t first_pages = 0;  // pages of the first interval (each chain's last page counted whole)
+    for (size_t i = 0; i < n; ++i) first_pages += tape_pages_for(c->adj_nsteps_h[i], c->adj_nsegs_h[i]);
+    const double projected = (double)first_pages * (double)count;
+    if (projected <= 0.9 * (double)c->tape_pages) {
+      t.append = 1;  // the whole tape should fit: continue the chains
+      ST_TRY(adj_record_launch(c, w_end, t, c->adj_nsteps_h, c->adj_nsegs_h));
+      ++launches;
+    } else {
+      tail_mode = true;
+      // keep room for the replay of one interval (chunks shrink to fit it), the
+      // tail takes the rest but for two partly filled pages per particle
+      const double reserve = 1.25 * (double)first_pages + 2.0 * (double)n;
+      int keep = (int)std::floor((0.9 * (double)c->tape_pages - reserve - 2.0 * (double)n) /
+                                 std::max<double>((double)first_pages, 1.0));
+      keep = std::max(0, std::min(keep, count - 1));
+      const int k_tail = count - keep;
+      if (k_tail > 1) {  // the middle, tape off
+        st::TapeArgs off = adj_record_args(c, 0);
+        ST_TRY(adj_record_launch(c, std::min(k_tail * every, w_end), off, c->adj_nsteps_h, c->adj_nsegs_h));
+        ++launches;
+      }
+      ST_TRY(adj_reset_tape(c, t));
+      if (keep > 0) {
+        ST_TRY(adj_record_launch(c, w_end, t, c->adj_nsteps_h, c->adj_nsegs_h));
+        ++launches;
+        c->adj_tail_from = k_tail;
+      }
+    }
+  } else {
+    ST_TRY(adj_record_launch(c, w_end, t, c->adj_nsteps_h, c->adj_nsegs_h));
+    ++launches;
+  }
   std::vector<int32_t> comp(std::max<size_t>(n, 1));
-  ST_CUDA(cudaMemcpyAsync(c->adj_nsteps_h.data(), t.nsteps, 8 * n, cudaMemcpyDeviceToHost, c->stream));
-  ST_CUDA(cudaMemcpyAsync(c->adj_nsegs_h.data(), t.nsegs, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  unsigned long long head = 0;
   ST_CUDA(cudaMemcpyAsync(c->adj_stop_h.data(), c->s.stop, n, cudaMemcpyDeviceToHost, c->stream));
   ST_CUDA(cudaMemcpyAsync(comp.data(), t.complete, 4 * n, cudaMemcpyDeviceToHost, c->stream));
-  ST_TRY(end_run(c, 1));
+  ST_CUDA(cudaMemcpyAsync(&head, c->tail_head, sizeof(head), cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaStreamSynchronize(c->stream));
   c->fresh = false;
   c->window_grid = true;
-  bool resident = true;
+  bool stored = true;  // every live particle's chains of the last record launch complete
   uint64_t used = 0;
   for (size_t i = 0; i < n; ++i) {
     used += (uint64_t)tape_pages_for(c->adj_nsteps_h[i], c->adj_nsegs_h[i]) * kPageBytes;
-    if (!c->adj_stop_h[i] && !comp[i]) resident = false;
+    if (!c->adj_stop_h[i] && !comp[i]) stored = false;
   }
+  const bool resident = stored && !tail_mode;
+  if (tail_mode && stored && c->adj_tail_from < count) {
+    c->adj_tail_pages = std::min<int64_t>((int64_t)head, c->tape_pages);
+  } else {
+    c->adj_tail_from = count;  // nothing kept apart from a resident tape
+  }
+  if (resident) c->adj_tail_pages = c->tape_pages;  // the record's chains hold all of it
   std::vector<int64_t> all(n);
   for (size_t i = 0; i < n; ++i) all[i] = (int64_t)i;
   ST_TRY(adj_upload_order(c, all, c->adj_order));
@@ -1219,6 +1308,8 @@ int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_c
   c->adj_stats.resident = resident ? 1 : 0;
   c->adj_stats.checkpoints = count;
   c->adj_stats.windows_per_checkpoint = every;
+  c->adj_stats.tail_from = c->adj_tail_from;
+  c->adj_stats.record_launches = launches;
   return ST_OK;
 }
 
@@ -1252,11 +1343,16 @@ int st_adjoint_backward_multi(st_ctx* c, int nloss, const double* dL_dS, double*
   ST_CUDA(cudaMemcpyAsync(c->adj_lam_buf, dL_dS, sizeof(double) * lam_d, cudaMemcpyDeviceToDevice, c->stream));
   ST_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * st::kNumTheta * n * (size_t)nloss, c->stream));
   ST_CUDA(cudaMemsetAsync(c->tape_error, 0, sizeof(long long) * st::kTapeErrorSlots, c->stream));
-  if (c->adj_resident) {
+  if (c->adj_resident || c->adj_tail_from < c->ckpt_count) {
+    // the record pass's own tape: all of it, or its last intervals
+    st::TapeArgs tr = adj_record_args(c, c->adj_tail_pages);
+    tr.final_stop = t.final_stop;
+    tr.pulse_grads = t.pulse_grads;
     st::RunArgs a = make_args(c, 0, c->adj_w_end, nullptr);
     a.order = c->adj_order;
     a.nitems = c->n;
-    return adj_backward_losses(c, a, t);
+    ST_TRY(adj_backward_losses(c, a, tr));
+    if (c->adj_resident) return ST_OK;
   }
   // replay chunks of checkpoint intervals, last first, each sized from the
   // record pass's tape length (time-uniform estimate; halves when it misses)
@@ -1267,14 +1363,13 @@ int st_adjoint_backward_multi(st_ctx* c, int nloss, const double* dL_dS, double*
     ++live;
   }
   const double per_interval = (double)total_pages / (double)c->ckpt_count + 2.0 * (double)live;
-  int k_hi = c->ckpt_count;
+  int k_hi = c->adj_tail_from;  // intervals before the kept tail
   while (k_hi > 0) {
-    int span = (int)std::floor(0.85 * (double)c->tape_pages / std::max(per_interval, 1.0));
+    int span = (int)std::floor(0.85 * (double)adj_replay_pages(c) / std::max(per_interval, 1.0));
     span = std::max(1, std::min(span, k_hi));
     ST_TRY(adj_chunk(c, k_hi - span, k_hi, t));
     k_hi -= span;
   }
-  c->adj_resident = false;  // the pool now holds a replay's tape
   return ST_OK;
 }
 

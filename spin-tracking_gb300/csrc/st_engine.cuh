@@ -361,6 +361,22 @@ __device__ __forceinline__ void tape_seg(const TapeArgs& t, TapeCursor& c, const
   }
 }
 
+// A particle's cursor at fetch: fresh chains, or (append) the chains the
+// previous launch closed, continued.
+__device__ __forceinline__ void tape_resume(const TapeArgs& t, TapeCursor& c, int64_t i) {
+  if (!t.append) {
+    tape_open(c);
+    return;
+  }
+  c.sp = t.step_page[i];
+  c.sf = c.sp < 0 ? kTapeStepsPerPage : t.step_fill[i];
+  c.gp = t.seg_page[i];
+  c.gf = c.gp < 0 ? kTapeSegsPerPage : t.seg_fill[i];
+  c.ns = t.nsteps[i];
+  c.ng = t.nsegs[i];
+  c.ok = t.complete[i] != 0;
+}
+
 __device__ __forceinline__ void tape_close(const TapeArgs& t, const TapeCursor& c, int64_t i) {
   t.step_page[i] = c.sp;
   t.step_fill[i] = c.sp < 0 ? 0 : c.sf;
@@ -467,7 +483,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
         P = &a.sets[a.s.set[i]];
         w = a.s.w_done[i];
         wlast = min(a.w_end, P->nwin);
-        if (TAPE) tape_open(tc);
+        if (TAPE) tape_resume(ta, tc, i);
         dd.pending = false;
         if (w >= wlast) {
           if (TAPE) tape_close(ta, tc, i);

@@ -132,6 +132,7 @@ struct TapeArgs {
   int32_t *seg_page, *seg_fill;   // last page of the segment chain and its records
   int64_t *nsteps, *nsegs;        // records of each chain, counted even when not stored
   int32_t* complete;              // 1: both chains stored in full
+  int append;                     // 1: continue each particle's chains from the cursors of the last close
   // state checkpoints written at window ends (record pass): state k is the
   // state after window k * ckpt_every - 1, at ckpt.<field> + k * ckpt_stride bytes
   DeviceState ckpt;

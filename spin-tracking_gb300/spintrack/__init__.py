@@ -255,3 +255,8 @@ def main_analysis(opt: Options, out_path: str | Path, kernel: int = KERNEL_PERSI
     secs = ctypes.c_double()
     check(load().st_main_analysis(ctypes.byref(opt), str(out_path).encode(), device, int(kernel), ctypes.byref(secs)))
     return secs.value
+
+
+def variant_name(variant: int) -> str:
+    """Name of a persistent-kernel launch variant (st_launch_variant_name)."""
+    return load().st_launch_variant_name(int(variant)).decode()

@@ -57,7 +57,8 @@ class AdjointStats(ctypes.Structure):
     """st_adjoint_stats."""
     _fields_ = [("tape_bytes_used", c_uint64), ("tape_bytes_pool", c_uint64), ("resident", ctypes.c_int32),
                 ("checkpoints", ctypes.c_int32), ("windows_per_checkpoint", ctypes.c_int32),
-                ("replays", ctypes.c_int32), ("groups", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("replays", ctypes.c_int32), ("groups", ctypes.c_int32), ("tail_from", ctypes.c_int32),
+                ("record_launches", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class Ensemble(ctypes.Structure):
