@@ -30,6 +30,16 @@
 //                                     sanity_check (src/particle.cpp:121-444)
 //                                     with tf = opt.tf; prints per segment
 //                                     coll_type wall_hit dt t pos v next_gas
+//   ref_probe spectrum PARAMS ax ay az wx wy wz
+//                                     integratorType 6 (noise amplitudes a and
+//                                     frequencies w set, the params file has no
+//                                     keys for them): floquet_diagonalize
+//                                     (src/integrator.cpp:824) frequencies and
+//                                     dt, then per particle the first window of
+//                                     runSimulationCPU's loop (src/particle.cpp:
+//                                     746-800) with integrateSpectrum, and the
+//                                     aggregator's state at its end: samples,
+//                                     bounces, collisions, s1, s2, imag_diag
 #include "include/particle.h"
 #include "include/optionsParser.h"
 #include "include/integrator.h"
@@ -68,8 +78,19 @@ struct Arrays {
   }
 };
 
-static void init_all(const options& opt, Arrays& a) {
-  floquetDiagonalization fd{};
+// SpectrumAggregator's members in their declaration order (include/floquet.h:
+// 76-95), to read the private accumulators of an aggregator the reference ran.
+struct SpecMirror {
+  int n_samples;
+  coords s1[NW];
+  coords s2[NW];
+  covMat cmat[NW];
+  double w[NW];
+  double dt;
+};
+static_assert(sizeof(SpecMirror) == sizeof(SpectrumAggregator), "SpectrumAggregator layout");
+
+static void init_all(const options& opt, Arrays& a, floquetDiagonalization fd = floquetDiagonalization{}) {
   initParticlesCPU(opt, a.S.data(), a.v.data(), a.v_old.data(), a.pos.data(), a.pos_old.data(),
                    a.t.data(), a.t_old.data(), a.tf.data(), a.dt.data(), a.next_gas.data(), a.h.data(),
                    a.state.data(), a.n_bounce.data(), a.n_coll.data(), a.n_steps.data(), a.partID.data(),
@@ -125,6 +146,44 @@ int main(int argc, char** argv) {
           std::printf(" %llu\n", (unsigned long long)s.x);
         }
       }
+    }
+    return 0;
+  }
+  if (!std::strcmp(cmd, "spectrum")) {
+    if (argc < 9) { std::fprintf(stderr, "spectrum needs 6 numbers\n"); return 2; }
+    opt.noiseAmplitudes = {std::strtod(argv[3], nullptr), std::strtod(argv[4], nullptr), std::strtod(argv[5], nullptr)};
+    opt.noiseFrequencies = {std::strtod(argv[6], nullptr), std::strtod(argv[7], nullptr), std::strtod(argv[8], nullptr)};
+    floquetDiagonalization fd = floquet_diagonalize(opt);
+    std::printf("f");
+    for (int k = 0; k < NW; ++k) hx(fd.frequencies[k]);
+    hx(fd.dt);
+    std::printf("\n");
+    Arrays a(opt.numParticles);
+    init_all(opt, a, fd);
+    for (int i = 0; i < a.n; ++i) {
+      SpectrumAggregator specagg = a.spec[i];
+      specagg.reset();
+      const double tf = opt.ioutInt;  // the first window
+      double t = a.t[i], t_old = a.t_old[i], ng = a.next_gas[i], dt = 0.0, tempH = a.h[i];
+      coords pos = a.pos[i], pos_old = a.pos_old[i], v = a.v[i], v_old = a.v_old[i];
+      rngState st = a.state[i];
+      size_t nb = 0, nc = 0;
+      char ct = 'W', wh = 0;
+      bool fin = false, stop = false;
+      int fail = 0;
+      while (!fin && !stop) {
+        calc_next_collision_time(t, tf, v, pos, ng, dt, ct, nb, nc, fin, wh, st, opt);
+        update_position_and_velocity(t_old, t, dt, pos_old, pos, v_old, v, ct, wh, st, stop, opt);
+        sanity_check(t_old, t, pos_old, pos, v, v_old, ct, wh, stop, fail, opt);
+        if (fail == 0) integrateSpectrum(t_old, t, specagg, pos_old, pos, v_old, v, opt, tempH);
+      }
+      SpecMirror m;
+      std::memcpy(&m, &specagg, sizeof(m));
+      std::printf("p %d %d %d %llu %llu", i, m.n_samples, fail, (unsigned long long)nb, (unsigned long long)nc);
+      for (int k = 0; k < NW; ++k) { hx(m.s1[k].x); hx(m.s1[k].y); hx(m.s1[k].z); }
+      for (int k = 0; k < NW; ++k) { hx(m.s2[k].x); hx(m.s2[k].y); hx(m.s2[k].z); }
+      for (int k = 0; k < NW; ++k) { hx(m.cmat[k].imag_diag.x); hx(m.cmat[k].imag_diag.y); hx(m.cmat[k].imag_diag.z); }
+      std::printf("\n");
     }
     return 0;
   }

@@ -391,6 +391,7 @@ int or_particles_alloc(or_particles *p, int n) {
 }
 
 void or_particles_free(or_particles *p) {
+  free(p->spec);
   free(p->S); free(p->v); free(p->v_old); free(p->pos); free(p->pos_old); free(p->t); free(p->t_old);
   free(p->h); free(p->next_gas); free(p->rng); free(p->fail); free(p->n_bounce); free(p->n_coll);
   free(p->n_steps); free(p->stop); free(p->coll_type); free(p->wall_hit);
@@ -1144,6 +1145,102 @@ int or_event(const or_options *o, or_particles *p, int i, double tf) {
   return finished;
 }
 
+/* ------------------------------------------------------------ integratorType 6
+ * integrateHamiltonian (src/integrator.cpp:745-785): y = q1 q2 ... q11 y per
+ * step, q_r the rotation of the CFET8 exponent with row r of G taken forwards
+ * (q1..q6) or row 12 - r backwards (q7..q11), the field at the Gauss-Legendre
+ * nodes from a particle at rest at the origin (findCrossTerm with zero p, v). */
+static int hamiltonian(const or_options *o, double t0, double tf, or_quat *y, double h) {
+  const or_vec3 zero = v3(0.0, 0.0, 0.0);
+  double t = t0;
+  unsigned int nstep = 0;
+  while (t < tf) {
+    nstep++;
+    if (nstep > o->nmax) return -2;
+    double rest = tf - t;
+    if (h >= rest) h = rest;
+    or_vec3 B[5];
+    for (int i = 0; i < 5; ++i) B[i] = omega(o, t + gl5_X[i] * h, t0, &zero, &zero);
+    or_quat q[12];
+    for (int r = 0; r < 5; ++r) q[11 - r] = rot_quat(magnus_exponent(cfet8_G[r], 1, B, 1.0), h);  /* q11..q7 */
+    for (int r = 5; r >= 0; --r) q[r + 1] = rot_quat(magnus_exponent(cfet8_G[r], 0, B, 1.0), h);  /* q6..q1 */
+    or_quat prod = qmul(q[1], q[2]);
+    for (int r = 3; r <= 11; ++r) prod = qmul(prod, q[r]);
+    *y = qmul(prod, *y);
+    t += h;
+  }
+  return 0;
+}
+
+void or_floquet_frequencies(const or_options *o, double freq[OR_NW], double *dt) {
+  const double t0 = 0.0, tf = (2 * M_PI) / o->w;
+  const int n_prop = 100;
+  or_quat y = {1.0, 0.0, 0.0, 0.0};
+  for (int i = 0; i < n_prop; ++i) {
+    double t1 = t0 + (tf - t0) * i / n_prop;
+    double t2 = t0 + (tf - t0) * (i + 1) / n_prop;
+    hamiltonian(o, t1, t2, &y, 1e-6);
+  }
+  /* qEigenval (src/quaternion.cpp:169-172) of the period's propagator */
+  const double ez = -sqrt(1.0 - y.w * y.w);
+  const double ea = fabs(atan2(ez, y.w)) / (tf - t0);
+  const double eb = -ea;
+  const double deltaE = ea - eb;
+  for (int k = 0; k <= 11 / 2; ++k)
+    for (int i = -1; i < 2; ++i) {
+      const int index = k * 3 + i;
+      if (index >= 0) freq[index] = deltaE * i + k * o->w;
+    }
+  *dt = (tf - t0) / n_prop;
+}
+
+static void spec_reset(or_spec *g) { memset(g, 0, sizeof(*g)); }
+
+/* goertzel_stage_1 and goertzel_stage_2_vector (src/floquet.cpp:25-38) per
+ * frequency, and covMat::add_outer (:107-110) with v = x (real), which adds
+ * 2 (b x - a 0) to the diagonal's imaginary part. */
+void or_spec_update(or_spec *g, const double freq[OR_NW], double dt, or_vec3 x) {
+  for (int i = 0; i < OR_NW; ++i) {
+    const double angle = freq[i] * dt;
+    const or_vec3 ns = vsub(vadd(x, vscale(2 * cos(angle), g->s1[i])), g->s2[i]);
+    g->s2[i] = g->s1[i];
+    g->s1[i] = ns;
+    const double angle2 = freq[i] * dt;
+    const or_vec3 b = vscale(sin(angle2), g->s2[i]);
+    const or_vec3 bx = v3(b.x * x.x, b.y * x.y, b.z * x.z);
+    const or_vec3 ax0 = v3(0.0, 0.0, 0.0);  /* a * imag(v) with v real */
+    g->imag[i] = vadd(g->imag[i], vscale(2, vsub(bx, ax0)));
+  }
+  g->n_samples += 1;
+}
+
+const or_spec *or_spectrum_of(const or_particles *p, int i) { return p->spec ? &p->spec[i] : NULL; }
+
+/* integrateSpectrum (src/integrator.cpp:724-743): samples on the grid of
+ * multiples of h inside (t0, tf], each the noise field findNoiseTerm (:72-80)
+ * halved: gamma (v x E / c^2 + grad(p) + testNoise(t)) / 2. */
+static int integrate_spectrum(const or_options *o, double t0, double tf, or_spec *g, const double freq[OR_NW],
+                              double fdt, const or_vec3 *p_old, const or_vec3 *v_old, double h) {
+  double t = (floor(t0 / h) + 1) * h;
+  const double next_t = (floor(tf / h) + 1) * h;
+  int n = 0;
+  while (t < next_t - (h / 2)) {
+    or_vec3 p, v;
+    or_interpolate(o, t, t0, p_old, v_old, &p, &v);
+    const or_vec3 G = v3(vdot(p, o->Gx), vdot(p, o->Gy), vdot(p, o->Gz));
+    const or_vec3 a = o->noiseAmplitudes, w = o->noiseFrequencies;
+    const or_vec3 N = v3(a.x * sin(w.x * t), a.y * sin(w.y * t), a.z * sin(w.z * t));
+    const or_vec3 B = vadd(vadd(vscale(1.0 / OR_C2, vcross(v, o->E)), G), N);
+    or_spec_update(g, freq, fdt, vdivs(vscale(o->gamma, B), 2));
+    t += h;
+    n++;
+  }
+  return n;
+}
+
+/* The frequencies of the running window loop (integratorType 6). */
+static double g_spec_freq[OR_NW], g_spec_dt;
+
 /* The per-particle window loop of runSimulationCPU (src/particle.cpp:722-803). */
 static void run_particle(const or_options *o, or_particles *p, int i, double next_t, uint64_t *nseg) {
   double tf = next_t;
@@ -1160,6 +1257,9 @@ static void run_particle(const or_options *o, or_particles *p, int i, double nex
         res = or_integrate_rk45(o, p->t_old[i], p->t[i], &p->S[i], &p->pos_old[i], &p->v_old[i], &hcarry);
       else if (o->integratorType >= 2 && o->integratorType <= 5)
         res = or_integrate_ext(o, p->t_old[i], p->t[i], &p->S[i], &p->pos_old[i], &p->v_old[i], &hcarry);
+      else if (o->integratorType == 6 && p->spec)
+        integrate_spectrum(o, p->t_old[i], p->t[i], &p->spec[i], g_spec_freq, g_spec_dt, &p->pos_old[i],
+                           &p->v_old[i], hcarry);
       if (o->keepStepSize) p->h[i] = hcarry;
       if (res < 0) {
         p->stop[i] = true;
@@ -1178,6 +1278,11 @@ static void run_particle(const or_options *o, or_particles *p, int i, double nex
 
 void or_run_until(const or_options *o, or_particles *p, double next_t, int nthreads) {
   uint64_t nseg = 0;
+  if (o->integratorType == 6) {  /* the aggregators restart every window (src/particle.cpp:746-747) */
+    if (!p->spec) p->spec = calloc(p->n > 0 ? (size_t)p->n : 1, sizeof(or_spec));
+    for (int i = 0; i < p->n; ++i) spec_reset(&p->spec[i]);
+    or_floquet_frequencies(o, g_spec_freq, &g_spec_dt);
+  }
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1) reduction(+ : nseg)

@@ -52,7 +52,18 @@ typedef struct {
   uint64_t *n_bounce, *n_coll, *n_steps;
   bool *stop;
   char *coll_type, *wall_hit;
+  struct or_spec *spec;  /* integratorType 6: one noise-spectrum aggregator per particle (allocated by or_init) */
 } or_particles;
+
+/* Noise-spectrum aggregator of integratorType 6 (SpectrumAggregator,
+ * include/floquet.h:76-95): per Goertzel frequency, the recursion's last two
+ * values s1, s2 and the Laplace term of the covariance diagonal (covMat
+ * imag_diag; its other members stay zero), and the samples taken. */
+#define OR_NW 17
+typedef struct or_spec {
+  or_vec3 s1[OR_NW], s2[OR_NW], imag[OR_NW];
+  int64_t n_samples;
+} or_spec;
 
 size_t or_options_size(void);
 void or_options_default(or_options *opt);
@@ -125,6 +136,16 @@ int64_t or_step_log_count(void);
  * first (mode 3: the picked one), the particle time at the start of its
  * segment, the function (OR_FN_*) and the argument; null arrays turn the
  * audit off. */
+/* floquet_diagonalize (src/integrator.cpp:824-867): the 17 Goertzel
+ * frequencies and the step dt of the dressed-spin Floquet analysis, from the
+ * one-period propagator of the field gamma (B0 + pulse) (integrateHamiltonian,
+ * src/integrator.cpp:745-785, 100 intervals of 1e-6 s Magnus CFET8 steps). */
+void or_floquet_frequencies(const or_options *opt, double freq[OR_NW], double *dt);
+/* SpectrumAggregator::update (src/floquet.cpp:113-120) with the sample x. */
+void or_spec_update(or_spec *g, const double freq[OR_NW], double dt, or_vec3 x);
+/* The aggregator of local particle slot i (after or_run_until). */
+const or_spec *or_spectrum_of(const or_particles *p, int i);
+
 enum { OR_FN_LOG = 0, OR_FN_SIN = 1, OR_FN_COS = 2, OR_FN_ACOS = 3 };
 void or_set_math_mode(int mode);
 void or_set_math_pick(const int64_t *k);

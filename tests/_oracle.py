@@ -26,12 +26,21 @@ class Rng(ctypes.Structure):
                 ("has_spare", ctypes.c_bool)]
 
 
+NW = 17  # Goertzel frequencies of integratorType 6
+
+
+class Spec(ctypes.Structure):
+    """or_spec: one particle's noise-spectrum aggregator."""
+    _fields_ = [("s1", Vec3 * NW), ("s2", Vec3 * NW), ("imag", Vec3 * NW), ("n_samples", ctypes.c_int64)]
+
+
 class Particles(ctypes.Structure):
     _fields_ = [("n", c_int)] + [(k, POINTER(Vec3)) for k in ("S", "v", "v_old", "pos", "pos_old")] + \
                [(k, POINTER(c_double)) for k in ("t", "t_old", "h", "next_gas")] + \
                [("rng", POINTER(Rng)), ("fail", POINTER(c_int))] + \
                [(k, POINTER(c_uint64)) for k in ("n_bounce", "n_coll", "n_steps")] + \
-               [("stop", POINTER(ctypes.c_bool)), ("coll_type", POINTER(c_char)), ("wall_hit", POINTER(c_char))]
+               [("stop", POINTER(ctypes.c_bool)), ("coll_type", POINTER(c_char)), ("wall_hit", POINTER(c_char)),
+                ("spec", POINTER(Spec))]
 
 
 class Counters(ctypes.Structure):
@@ -75,6 +84,7 @@ class Oracle:
             "or_set_counters": (None, [c_void_p]),
             "or_set_step_log": (None, [c_void_p, ctypes.c_int64, c_int]),
             "or_step_log_count": (ctypes.c_int64, []),
+            "or_floquet_frequencies": (None, [P(Options), P(c_double), P(c_double)]),
             "or_set_math_mode": (None, [c_int]),
             "or_set_math_pick": (None, [c_void_p]),
             "or_set_math_audit": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
@@ -146,6 +156,39 @@ class Oracle:
             self.L.or_set_math_pick(None)
             self.L.or_set_math_mode(self.MATH_LIBM)
         return secs, out, {"count": cnt, "first_t": t1, "first_fn": fn, "first_arg": arg}
+
+    # integratorType 6: noise spectrum -----------------------------------
+    def floquet_frequencies(self, opt: Options):
+        """floquet_diagonalize's 17 Goertzel frequencies and dt."""
+        import numpy as np
+        f = (c_double * NW)()
+        dt = c_double()
+        self.L.or_floquet_frequencies(ctypes.byref(opt), f, ctypes.byref(dt))
+        return np.array(f[:]), dt.value
+
+    def run_spectrum(self, opt: Options, first: int, count: int, threads: int = 0):
+        """Particles [first, first + count) of a type-6 run through every
+        window; returns (arrays, spectrum) where spectrum holds each particle's
+        aggregator at the end of the last window: s1, s2, imag [count, 17, 3]
+        and n_samples [count]."""
+        import numpy as np
+        p = self.alloc(count)
+        try:
+            self.L.or_run_sample(ctypes.byref(opt), first, count, threads, ctypes.byref(p))
+            out = self.arrays(p)
+            spec = {"s1": np.zeros((count, NW, 3)), "s2": np.zeros((count, NW, 3)), "imag": np.zeros((count, NW, 3)),
+                    "n_samples": np.zeros(count, np.int64)}
+            if p.spec:
+                for i in range(count):
+                    g = p.spec[i]
+                    for k in range(NW):
+                        for name in ("s1", "s2", "imag"):
+                            v = getattr(g, name)[k]
+                            spec[name][i, k] = (v.x, v.y, v.z)
+                    spec["n_samples"][i] = g.n_samples
+        finally:
+            self.free(p)
+        return out, spec
 
     # options -------------------------------------------------------------
     def default_options(self) -> Options:

@@ -8,7 +8,9 @@ compiled unchanged against oracle/ref_stubs).  Writes, per case:
 and probe vectors (C99 hex floats) from oracle/_ref/ref_probe:
   probe_init_<dist>.txt, probe_draws.txt, probe_events.txt, probe_dop.txt,
   probe_rk45.txt, probe_magnus.txt, probe_rk45q.txt, probe_rkf45.txt,
-  probe_rkf45q.txt (single segments of every stepper)
+  probe_rkf45q.txt (single segments of every stepper),
+  probe_spectrum.txt, probe_spectrum_m.txt (integratorType 6: Floquet
+  frequencies and each particle's noise-spectrum aggregator after a window)
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -186,9 +188,38 @@ def main() -> int:
             for pz in variants:
                 lines.append(f"{pz.name} {' '.join(args)} | " + run([str(probe), cmd, str(pz), *args]).stdout.strip())
         (HERE / f"probe_{cmd}.txt").write_text("\n".join(lines) + "\n")
+    spectrum_probes(probe)
     print("probes written")
     return 0
 
 
+# integratorType 6 (the noise spectrum): a dressed run with gas, diffuse walls,
+# the full gradient tensor and a test noise field, and a Maxwell-Boltzmann run
+# with specular walls and no pulse amplitude (the Floquet period still comes
+# from w).  The noise amplitudes and frequencies follow the params file on the
+# probe's command line (the reference's parser has no keys for them).
+SPECTRUM_CASES = {
+    "probe_spectrum": (dict(numParticles="8", dist="C", V="5", gas_coll="true", T="0.4", diffuse="0.3",
+                            gravity="true", yi="0, 0, 1", a="5e-6", w="6283.185307179586", h="1e-5", tf="0.02",
+                            ioutInt="0.01", integratorType="6", seed="5", **G_FULL),
+                       ["1e-9", "2e-9", "0", "300", "700", "0"]),
+    "probe_spectrum_m": (dict(numParticles="8", dist="M", T="4.2", gas_coll="false", diffuse="0", gravity="true",
+                              yi="0, 0, 1", a="0", w="3141.592653589793", h="2e-5", tf="0.01", ioutInt="0.01",
+                              integratorType="6", seed="11", **G_FULL),
+                         ["0", "0", "0", "0", "0", "0"]),
+}
+
+
+def spectrum_probes(probe) -> None:
+    for name, (case, noise) in SPECTRUM_CASES.items():
+        p = HERE / f"{name}.params"
+        p.write_text(params_text(case))
+        out = run([str(probe), "spectrum", str(p), *noise]).stdout
+        (HERE / f"{name}.txt").write_text("noise " + " ".join(noise) + "\n" + out)
+
+
 if __name__ == "__main__":
+    if sys.argv[1:] == ["spectrum"]:  # only the integratorType 6 probes
+        spectrum_probes(ORACLE / "_ref" / "ref_probe")
+        sys.exit(0)
     sys.exit(main())

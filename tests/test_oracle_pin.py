@@ -430,3 +430,44 @@ def test_main_analysis_matches_reference_on_random_configurations(oracle, tmp_pa
         a, b = our_out.read_bytes(), ref_out.read_bytes()
         assert len(a) == len(b) and header_equal(a, b), params.read_text()
         assert a[440:] == b[440:], params.read_text()
+
+
+def spectrum_fixture(name):
+    """A probe_spectrum*.txt fixture: noise arguments, the Floquet frequencies
+    and dt, and per particle (samples, failure, bounces, collisions, s1, s2,
+    imag_diag) after the first window."""
+    lines = (GOLDEN / f"{name}.txt").read_text().splitlines()
+    noise = [float(x) for x in lines[0].split()[1:]]
+    f = [hexf(x) for x in lines[1].split()[1:]]
+    parts = []
+    for l in lines[2:]:
+        tok = l.split()
+        vals = np.array([hexf(x) for x in tok[6:]]).reshape(3, 17, 3)
+        parts.append({"i": int(tok[1]), "n_samples": int(tok[2]), "fail": int(tok[3]), "n_bounce": int(tok[4]),
+                      "n_coll": int(tok[5]), "s1": vals[0], "s2": vals[1], "imag": vals[2]})
+    return noise, np.array(f[:17]), f[17], parts
+
+
+@pytest.mark.parametrize("name", ["probe_spectrum", "probe_spectrum_m"])
+def test_spectrum_matches_reference(oracle, name):
+    """integratorType 6: floquet_diagonalize's frequencies and dt
+    (src/integrator.cpp:824-867) and every particle's noise-spectrum
+    aggregator (goertzel_stage_1/2_vector and covMat::add_outer,
+    src/floquet.cpp:25-45, 107-120, fed by integrateSpectrum,
+    src/integrator.cpp:730-743) after the first window, bit for bit."""
+    noise, freq, dt, parts = spectrum_fixture(name)
+    opt = oracle.parse_file(GOLDEN / f"{name}.params")
+    opt.noiseAmplitudes.x, opt.noiseAmplitudes.y, opt.noiseAmplitudes.z = noise[0:3]
+    opt.noiseFrequencies.x, opt.noiseFrequencies.y, opt.noiseFrequencies.z = noise[3:6]
+    f, d = oracle.floquet_frequencies(opt)
+    assert np.array_equal(f, freq) and d == dt
+    opt.tf = opt.ioutInt  # the probe ran the first window
+    out, spec = oracle.run_spectrum(opt, 0, opt.numParticles, threads=2)
+    assert len(parts) == opt.numParticles
+    for p in parts:
+        i = p["i"]
+        assert spec["n_samples"][i] == p["n_samples"] and out["fail"][i] == p["fail"]
+        assert out["n_bounce"][i] == p["n_bounce"] and out["n_coll"][i] == p["n_coll"]
+        for k in ("s1", "s2", "imag"):
+            assert np.array_equal(spec[k][i], p[k]), (i, k)
+    assert min(p["n_samples"] for p in parts) > 400
