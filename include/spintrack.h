@@ -313,6 +313,36 @@ int st_probe_fp64_peak(int device, double *tflops);
  * For tests; no reference counterpart. */
 int st_crmath_eval(int fn, const double *x, double *y, int64_t n);
 
+/* ---- integratorType 6: the noise spectrum ------------------------------- */
+/* A context whose sets all have integratorType 6 integrates no spin: along
+ * every segment it samples the noise field gamma (v x E / c^2 + grad(p) +
+ * testNoise(t)) / 2 on the grid of multiples of h and runs 17 Goertzel
+ * recursions per particle, at the Floquet frequencies of the dressed spin
+ * (integrateSpectrum and SpectrumAggregator, src/integrator.cpp:724-743,
+ * src/floquet.cpp:25-156); the aggregators restart at every window, as the
+ * reference's window loop resets them (src/particle.cpp:746-747).  Type 6 sets
+ * need w != 0 and cannot share a context with types 0-5; both kernel
+ * selectors run the spectrum kernel. */
+#define ST_SPECTRUM_FREQS 17
+/* floquet_diagonalize (src/integrator.cpp:824-867): the 17 Goertzel
+ * frequencies (rad/s) and the Goertzel step dt of opt's dressing field. */
+int st_floquet_frequencies(const st_options *opt, double *freq, double *dt);
+/* Every particle's aggregator after the last window: host arrays of
+ * numParticles x 17 x 3 doubles (s1, s2: the recursion's last two values;
+ * imag: the Laplace term of the covariance diagonal, covMat::imag_diag) and
+ * the samples taken.  The reference keeps them in SpectrumAggregator
+ * (include/floquet.h:76-95, particle::getSpectrumAggregators). */
+int st_spectrum_state(st_ctx *ctx, double *s1, double *s2, double *imag, int64_t *n_samples);
+/* The covariance spectrum of a set summed over its particles in index order:
+ * variance[k][r][q] (complex, 17 x 3 x 3 x {re, im}) = sum over particles of
+ * c_r conj(c_q) with c = s1 - cos(w_k dt) s2 + i sin(w_k dt) s2, minus i imag
+ * on the diagonal (goertzel_stage_2 and get_covariance_spectrum,
+ * src/floquet.cpp:40-47, 130-145; CovarianceSpectrum::add, :74-79).  The
+ * reference's own reduction nests its tree loops the wrong way round
+ * (src/particle.cpp:826-834) and its GPU path does not reduce; this is the
+ * plain sum they aim at, unnormalised, with the samples in *n_samples. */
+int st_covariance_spectrum(st_ctx *ctx, int set, double *variance, int64_t *n_samples);
+
 /* ---- driver: mainAnalysis (src/simulation.cpp:8-96) -------------------- */
 /* Derive tc/sqrtKT_m, create, init, write the options header and the t0
  * snapshot, run every window with `kernel`, append a snapshot per window

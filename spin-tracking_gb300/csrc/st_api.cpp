@@ -97,8 +97,8 @@ bool to_bool(const std::string& s) {
 // ---------------------------------------------------------------- params
 int build_params(const st_options& o, int64_t first, SetParams* P) {
   if (o.numParticles < 0) return fail(ST_ERR_ARG, "numParticles must be >= 0");
-  if (o.integratorType == 6)
-    return fail(ST_ERR_UNSUPPORTED, "integratorType 6 (spectrum) is not implemented; use 0-5");
+  if (o.integratorType == 6 && !(o.w != 0.0 && std::isfinite(o.w)))
+    return fail(ST_ERR_ARG, "integratorType 6 needs a nonzero pulse frequency w: its Floquet period is 2 pi / w");
   if (o.dist != 'C' && o.dist != 'M')
     return fail(ST_ERR_UNSUPPORTED, std::string("dist must be 'C' or 'M', got '") + o.dist + "'");
   if (!(o.ioutInt > 0.0)) return fail(ST_ERR_ARG, "ioutInt must be > 0");
@@ -180,6 +180,11 @@ struct st_ctx {
   };
   std::vector<RunGraph> graphs;
   void* ens_buf = nullptr;   // ensemble statistics: control slots, block partials, histogram
+  // integratorType 6 (every set of the context): the noise-spectrum aggregators
+  bool spectrum = false;
+  st::SpecSet* spec_sets_d = nullptr;
+  void* spec_pp = nullptr;        // s1, s2, im (17 x 3 per particle each), samples per particle
+  st::SpecArgs spec{};
   // adjoint (allocated by st_adjoint_record)
   double* tape_pool = nullptr;
   int32_t* tape_prev = nullptr;
@@ -270,6 +275,23 @@ int ctx_alloc(st_ctx* c) {
     off += align256(esz[k] * m);
   }
   c->snap.bytes = off;
+  if (c->spectrum) {  // integratorType 6: the Floquet frequencies per set and the aggregators
+    std::vector<st::SpecSet> q(c->opts.size());
+    for (size_t k = 0; k < c->opts.size(); ++k)
+      if (st::build_spec_set(c->opts[k], &q[k]) != 0) return fail(ST_ERR_ARG, "integratorType 6: no Floquet period");
+    ST_CUDA(cudaMalloc(&c->spec_sets_d, sizeof(st::SpecSet) * q.size()));
+    ST_CUDA(cudaMemcpyAsync(c->spec_sets_d, q.data(), sizeof(st::SpecSet) * q.size(), cudaMemcpyHostToDevice,
+                            c->stream));
+    const size_t acc = align256(sizeof(double) * 3 * st::kSpecFreqs * m);
+    ST_CUDA(cudaMalloc(&c->spec_pp, 3 * acc + align256(8 * m)));
+    ST_CUDA(cudaMemsetAsync(c->spec_pp, 0, 3 * acc + align256(8 * m), c->stream));
+    char* b = (char*)c->spec_pp;
+    c->spec.sets = c->spec_sets_d;
+    c->spec.s1 = (double*)b;
+    c->spec.s2 = (double*)(b + acc);
+    c->spec.im = (double*)(b + 2 * acc);
+    c->spec.nsamp = (int64_t*)(b + 3 * acc);
+  }
   ST_CUDA(cudaStreamSynchronize(c->stream));
   return ST_OK;
 }
@@ -588,8 +610,13 @@ int st_create_batch(const st_options* sets, int nsets, int device, st_ctx** out)
     c->opts.push_back(sets[k]);
     c->sets_h.push_back(P);
     first += sets[k].numParticles;
+    if ((sets[k].integratorType == 6) != (sets[0].integratorType == 6)) {
+      delete c;
+      return fail(ST_ERR_UNSUPPORTED, "integratorType 6 sets cannot share a context with spin-integrating sets");
+    }
   }
   c->n = first;
+  c->spectrum = sets[0].integratorType == 6;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
@@ -621,6 +648,8 @@ void st_destroy(st_ctx* c) {
   cudaFree(c->order_d);
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   cudaFree(c->ens_buf);
+  cudaFree(c->spec_sets_d);
+  cudaFree(c->spec_pp);
   cudaFree(c->adj_lam_buf);
   cudaFree(c->tape_pool);
   cudaFree(c->tape_prev);
@@ -657,7 +686,8 @@ int st_run_until(st_ctx* c, double next_t) {
   ST_TRY(arm_deadline(c, a));
   c->fresh = false;
   c->adj_recorded = false;
-  int e = st::launch_until(a, next_t, plain_block(c), c->stream);
+  int e = c->spectrum ? st::launch_spectrum(a, -1, next_t, c->spec, c->stream)
+                      : st::launch_until(a, next_t, plain_block(c), c->stream);
   if (e) return fail(ST_ERR_CUDA, std::string("plain launch: ") + cudaGetErrorString((cudaError_t)e));
   c->window_grid = false;
   return end_run(c, 1);
@@ -669,11 +699,12 @@ constexpr size_t kMaxRunGraphs = 8;
 // The launches of one st_run_windows call, enqueued on the context's stream.
 int enqueue_run(st_ctx* c, int kernel, int w_begin, int w_end, void* snap, int* launches) {
   ST_CUDA(cudaMemsetAsync(c->status_d, 0, sizeof(st::RunStatus), c->stream));
-  if (kernel == ST_KERNEL_PLAIN) {
+  if (kernel == ST_KERNEL_PLAIN || c->spectrum) {  // integratorType 6 runs its own kernel, window by window
     st::RunArgs a = make_args(c, w_begin, w_end, snap);
     ST_TRY(arm_deadline(c, a));
     for (int w = w_begin; w < w_end; ++w) {
-      int e = st::launch_plain_window(a, w, plain_block(c), c->stream);
+      int e = c->spectrum ? st::launch_spectrum(a, w, 0.0, c->spec, c->stream)
+                          : st::launch_plain_window(a, w, plain_block(c), c->stream);
       if (e) return fail(ST_ERR_CUDA, std::string("plain launch: ") + cudaGetErrorString((cudaError_t)e));
       ++*launches;
       if (snap) {
@@ -698,7 +729,7 @@ int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
   if (kernel != ST_KERNEL_PLAIN && kernel != ST_KERNEL_PERSISTENT) return fail(ST_ERR_ARG, "unknown kernel selector");
   if (w_end == w_begin) return ST_OK;
   ST_CUDA(cudaSetDevice(c->device));
-  if (kernel == ST_KERNEL_PERSISTENT) {  // allocations and tuning happen outside the capture
+  if (kernel == ST_KERNEL_PERSISTENT && !c->spectrum) {  // allocations and tuning happen outside the capture
     ST_TRY(ctx_build_order(c));
     if (c->lc.variant < 0 || c->lc.blocks_per_sm <= 0) ST_TRY(autotune(c));
     if (int e = st::persistent_prepare(c->lc.variant))
@@ -706,9 +737,10 @@ int st_run_windows(st_ctx* c, int kernel, int w_begin, int w_end, void* snap) {
   }
   c->fresh = false;
   c->adj_recorded = false;
-  const int block = kernel == ST_KERNEL_PLAIN ? plain_block(c) : 0;
-  const int var = kernel == ST_KERNEL_PLAIN ? -1 : c->lc.variant;
-  const int bps = kernel == ST_KERNEL_PLAIN ? 0 : c->lc.blocks_per_sm;
+  const bool plain_shape = kernel == ST_KERNEL_PLAIN || c->spectrum;
+  const int block = plain_shape ? plain_block(c) : 0;
+  const int var = plain_shape ? -1 : c->lc.variant;
+  const int bps = plain_shape ? 0 : c->lc.blocks_per_sm;
   size_t hit = c->graphs.size();
   for (size_t k = 0; k < c->graphs.size(); ++k) {
     const auto& g = c->graphs[k];
@@ -829,8 +861,13 @@ int st_set_params(st_ctx* c, const st_options* sets, int nsets) {
   for (int k = 0; k < nsets; ++k) {
     if (sets[k].numParticles != c->opts[k].numParticles)
       return fail(ST_ERR_ARG, "st_set_params cannot change a set's particle count");
+    if ((sets[k].integratorType == 6) != c->spectrum)
+      return fail(ST_ERR_UNSUPPORTED, "st_set_params cannot switch between integratorType 6 and the spin integrators");
     ST_TRY(build_params(sets[k], c->sets_h[k].first, &P[k]));
   }
+  std::vector<st::SpecSet> q(c->spectrum ? (size_t)nsets : 0);
+  for (size_t k = 0; k < q.size(); ++k)
+    if (st::build_spec_set(sets[k], &q[k]) != 0) return fail(ST_ERR_ARG, "integratorType 6: no Floquet period");
   ST_CUDA(cudaSetDevice(c->device));
   // Captured run graphs hold the kernel instantiation chosen for the old sets
   // (with or without gas collisions, integrator types 2-5) and the work order
@@ -849,6 +886,9 @@ int st_set_params(st_ctx* c, const st_options* sets, int nsets) {
   ST_CUDA(cudaMemcpyAsync(c->sets_d, P.data(), sizeof(SetParams) * P.size(), cudaMemcpyHostToDevice, c->stream));
   if (int e = st::launch_prepare_sets(c->sets_d, nsets, c->stream))
     return fail(ST_ERR_CUDA, std::string("prepare sets: ") + cudaGetErrorString((cudaError_t)e));
+  if (!q.empty())
+    ST_CUDA(cudaMemcpyAsync(c->spec_sets_d, q.data(), sizeof(st::SpecSet) * q.size(), cudaMemcpyHostToDevice,
+                            c->stream));
   for (int k = 0; k < nsets; ++k) c->opts[k] = sets[k];
   c->sets_h = P;
   c->adj_recorded = false;  // a recorded tape belongs to the old parameters
@@ -1444,6 +1484,74 @@ int st_ensemble_stats(st_ctx* c, const void* snap, int set, st_ensemble* out) {
   const double phi0 = std::atan2(P.yi_z, P.yi_y);
   r.freq_shift_unwrapped = (r.phase_unwrapped_mean - (phi0 - w * r.t)) / r.t / (2.0 * pi);
   *out = r;
+  return ST_OK;
+}
+
+int st_floquet_frequencies(const st_options* opt, double* freq, double* dt) {
+  if (!opt || !freq || !dt) return fail(ST_ERR_ARG, "null argument");
+  if (st::floquet_frequencies(*opt, freq, dt) != 0)
+    return fail(ST_ERR_ARG, "integratorType 6 needs a nonzero pulse frequency w: its Floquet period is 2 pi / w");
+  return ST_OK;
+}
+
+int st_spectrum_state(st_ctx* c, double* s1, double* s2, double* imag, int64_t* n_samples) {
+  if (!c || !s1 || !s2 || !imag || !n_samples) return fail(ST_ERR_ARG, "null argument");
+  if (!c->spectrum) return fail(ST_ERR_STATE, "st_spectrum_state: the context's sets are not integratorType 6");
+  ST_CUDA(cudaSetDevice(c->device));
+  const size_t n = (size_t)c->n, f3 = 3 * (size_t)st::kSpecFreqs;
+  if (n == 0) return ST_OK;
+  // device arrays are field-major ([(k * 3 + c) * n + i]); the caller's are per particle ([i][k][c])
+  std::vector<double> buf(f3 * n);
+  double* dst[3] = {s1, s2, imag};
+  const double* src[3] = {c->spec.s1, c->spec.s2, c->spec.im};
+  for (int a = 0; a < 3; ++a) {
+    ST_CUDA(cudaMemcpyAsync(buf.data(), src[a], sizeof(double) * f3 * n, cudaMemcpyDeviceToHost, c->stream));
+    ST_CUDA(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < f3; ++j) dst[a][i * f3 + j] = buf[j * n + i];
+  }
+  ST_CUDA(cudaMemcpyAsync(n_samples, c->spec.nsamp, 8 * n, cudaMemcpyDeviceToHost, c->stream));
+  ST_CUDA(cudaStreamSynchronize(c->stream));
+  return ST_OK;
+}
+
+int st_covariance_spectrum(st_ctx* c, int set, double* variance, int64_t* n_samples) {
+  if (!c || !variance || !n_samples) return fail(ST_ERR_ARG, "null argument");
+  if (!c->spectrum) return fail(ST_ERR_STATE, "st_covariance_spectrum: the context's sets are not integratorType 6");
+  if (set < 0 || set >= (int)c->sets_h.size()) return fail(ST_ERR_ARG, "no such parameter set");
+  const size_t n = (size_t)c->n, F = st::kSpecFreqs;
+  std::vector<double> s1(3 * F * n), s2(3 * F * n), im(3 * F * n);
+  std::vector<int64_t> ns(std::max<size_t>(n, 1));
+  ST_TRY(st_spectrum_state(c, s1.data(), s2.data(), im.data(), ns.data()));
+  double fr[st::kSpecFreqs], dt = 0.0;
+  if (st::floquet_frequencies(c->opts[(size_t)set], fr, &dt) != 0) return fail(ST_ERR_ARG, "no Floquet period");
+  std::memset(variance, 0, sizeof(double) * F * 18);
+  int64_t total = 0;
+  const int64_t lo = c->sets_h[(size_t)set].first, hi = lo + c->sets_h[(size_t)set].n;
+  for (int64_t i = lo; i < hi; ++i) {  // particle order, so the sum does not depend on the launch
+    if (c->opts[(size_t)set].numParticles == 0) break;
+    total += ns[(size_t)i];
+    for (size_t k = 0; k < F; ++k) {
+      // goertzel_stage_2 (src/floquet.cpp:40-47): c = a + i b, variance = c c^dag,
+      // a = s1 - cos(w dt) s2, b = sin(w dt) s2; then the Laplace term on the
+      // diagonal (SpectrumAggregator::get_covariance_spectrum, :130-145)
+      const double angle = fr[k] * dt, ca = cos(angle), sa = sin(angle);
+      double re[3], imc[3];
+      for (int q = 0; q < 3; ++q) {
+        const double x1 = s1[((size_t)i * F + k) * 3 + q], x2 = s2[((size_t)i * F + k) * 3 + q];
+        re[q] = x1 - ca * x2;
+        imc[q] = sa * x2;
+      }
+      double* m = variance + k * 18;
+      for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) {  // c_r conj(c_q)
+          m[(r * 3 + q) * 2 + 0] += re[r] * re[q] + imc[r] * imc[q];
+          m[(r * 3 + q) * 2 + 1] += imc[r] * re[q] - re[r] * imc[q];
+        }
+      for (int r = 0; r < 3; ++r) m[(r * 3 + r) * 2 + 1] += -im[((size_t)i * F + k) * 3 + r];
+    }
+  }
+  *n_samples = total;
   return ST_OK;
 }
 

@@ -166,6 +166,28 @@ enum { ENS_COUNT = 0, ENS_SX, ENS_SY, ENS_SZ, ENS_MIN, ENS_MAX, ENS_T, ENS_EDGE0
 int launch_gather_phase(const double* Sy, const double* Sz, const int32_t* turns, int64_t n, double* dst,
                         void* stream);
 
+// integratorType 6 (st_spectrum.cu): the noise spectrum.  Per parameter set,
+// the Floquet frequencies of the Goertzel aggregators, the per-sample
+// constants 2 cos(w dt) and sin(w dt) as the reference evaluates them (on the
+// host), dt, and the test-noise amplitudes and frequencies; per particle, the
+// aggregators of the last window, field-major: s1[(k * 3 + c) * n + i].
+constexpr int kSpecFreqs = 17;
+constexpr int kSpecBlock = 128;  // four particles (warps) per block
+struct SpecSet {
+  double freq[kSpecFreqs], two_cos[kSpecFreqs], sin_a[kSpecFreqs];
+  double fdt;
+  double na[3], nw[3];
+};
+struct SpecArgs {
+  const SpecSet* sets;
+  double *s1, *s2, *im;
+  int64_t* nsamp;
+};
+// floquet_diagonalize's frequencies and dt (host); -1 when w gives no period.
+int floquet_frequencies(const st_options& o, double freq[kSpecFreqs], double* dt);
+int build_spec_set(const st_options& o, SpecSet* q);
+int launch_spectrum(const RunArgs& a, int window, double next_t, const SpecArgs& sp, void* stream);
+
 // Host-side launch helpers implemented in st_kernels.cu.  Return a cudaError_t
 // cast to int (0 = success).
 int launch_prepare_sets(SetParams* sets, int nsets, void* stream);

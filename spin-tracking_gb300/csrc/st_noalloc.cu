@@ -160,6 +160,8 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
   SetParams table[kNoAllocMaxSets];
   int64_t n = 0;
   for (int k = 0; k < nsets; ++k) {
+    if (sets[k].integratorType == 6)
+      return set_last_error(ST_ERR_UNSUPPORTED, "st_run_noalloc: integratorType 6 keeps per-particle spectra; use st_create");
     const int r = build_set_params(sets[k], n, &table[k]);
     if (r != ST_OK) return r;
     n += sets[k].numParticles;

@@ -151,6 +151,27 @@ class Particles:
     def set_deadline(self, seconds: float) -> None:
         check(load().st_set_deadline(self._ctx, float(seconds)))
 
+    def spectrum_state(self) -> dict:
+        """integratorType 6: every particle's noise-spectrum aggregator after the
+        last window (SpectrumAggregator, include/floquet.h:76-95): s1, s2,
+        imag [n, 17, 3] and n_samples [n]."""
+        n = self.n
+        out = {k: np.zeros((n, 17, 3)) for k in ("s1", "s2", "imag")}
+        out["n_samples"] = np.zeros(n, np.int64)
+        if n:
+            check(load().st_spectrum_state(self._ctx, out["s1"].ctypes.data, out["s2"].ctypes.data,
+                                           out["imag"].ctypes.data, out["n_samples"].ctypes.data))
+        return out
+
+    def covariance_spectrum(self, set_index: int = 0):
+        """integratorType 6: the set's covariance spectrum summed over its
+        particles, complex [17, 3, 3], and the samples it holds."""
+        v = np.zeros(17 * 18)
+        ns = np.zeros(1, np.int64)
+        check(load().st_covariance_spectrum(self._ctx, int(set_index), v.ctypes.data, ns.ctypes.data))
+        v = v.reshape(17, 3, 3, 2)
+        return v[..., 0] + 1j * v[..., 1], int(ns[0])
+
     def counters(self) -> dict:
         c = Counters()
         check(load().st_get_counters(self._ctx, ctypes.byref(c)))
@@ -260,3 +281,12 @@ def main_analysis(opt: Options, out_path: str | Path, kernel: int = KERNEL_PERSI
 def variant_name(variant: int) -> str:
     """Name of a persistent-kernel launch variant (st_launch_variant_name)."""
     return load().st_launch_variant_name(int(variant)).decode()
+
+
+def floquet_frequencies(opt):
+    """floquet_diagonalize (src/integrator.cpp:824-867): the 17 Goertzel
+    frequencies of opt's dressing field and the Goertzel step dt."""
+    f = (ctypes.c_double * 17)()
+    dt = ctypes.c_double()
+    check(load().st_floquet_frequencies(ctypes.byref(opt), f, ctypes.byref(dt)))
+    return np.array(f[:]), dt.value

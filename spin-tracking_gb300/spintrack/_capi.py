@@ -122,6 +122,9 @@ _SIGS = {
     "st_probe_fp64_peak": (c_int, [c_int, POINTER(c_double)]),
     "st_adjoint_record": (c_int, [c_void_p, c_int, c_size_t, c_int]),
     "st_adjoint_get_stats": (c_int, [c_void_p, POINTER(AdjointStats)]),
+    "st_floquet_frequencies": (c_int, [POINTER(Options), POINTER(c_double), POINTER(c_double)]),
+    "st_spectrum_state": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "st_covariance_spectrum": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "st_ensemble_stats": (c_int, [c_void_p, c_void_p, c_int, POINTER(Ensemble)]),
     "st_gather_phase": (c_int, [c_void_p, c_void_p]),
     "st_adjoint_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),

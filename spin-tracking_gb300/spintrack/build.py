@@ -21,8 +21,11 @@ LIB = BUILD / "libspintrack.so"
 CLI = BUILD / "spintrack"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
-UNITS = ["st_kernels.cu", "st_kernels_ext.cu", "st_api.cpp", "st_noalloc.cu", "st_adjoint.cu", "st_ensemble.cu"]
+# host code keeps the reference's rounding: no contraction of a * b + c into an FMA
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              f"-I{INCLUDE}", f"-I{CSRC}"]
+UNITS = ["st_kernels.cu", "st_kernels_ext.cu", "st_api.cpp", "st_noalloc.cu", "st_adjoint.cu", "st_ensemble.cu",
+         "st_spectrum.cu"]
 
 
 def _nvcc() -> str:

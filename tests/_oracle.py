@@ -166,13 +166,15 @@ class Oracle:
         self.L.or_floquet_frequencies(ctypes.byref(opt), f, ctypes.byref(dt))
         return np.array(f[:]), dt.value
 
-    def run_spectrum(self, opt: Options, first: int, count: int, threads: int = 0):
+    def run_spectrum(self, opt: Options, first: int, count: int, threads: int = 0, math_mode: int = 0):
         """Particles [first, first + count) of a type-6 run through every
         window; returns (arrays, spectrum) where spectrum holds each particle's
         aggregator at the end of the last window: s1, s2, imag [count, 17, 3]
-        and n_samples [count]."""
+        and n_samples [count].  math_mode: the trajectory's elementary
+        functions (MATH_LIBM, the reference's, or MATH_CR)."""
         import numpy as np
         p = self.alloc(count)
+        self.L.or_set_math_mode(math_mode)
         try:
             self.L.or_run_sample(ctypes.byref(opt), first, count, threads, ctypes.byref(p))
             out = self.arrays(p)
@@ -187,6 +189,7 @@ class Oracle:
                             spec[name][i, k] = (v.x, v.y, v.z)
                     spec["n_samples"][i] = g.n_samples
         finally:
+            self.L.or_set_math_mode(self.MATH_LIBM)
             self.free(p)
         return out, spec
 

@@ -127,7 +127,8 @@ def test_writer_layout(stlib, tmp_path):
     assert len(snaps) == 1 and np.array_equal(snaps[0]["n_steps"], ns) and np.array_equal(snaps[0]["S"], S)
 
 
-@pytest.mark.parametrize("field,value,code", [("integratorType", 6, _capi.ST_ERR_UNSUPPORTED),
+# integratorType 6 with the default w = 0: no Floquet period for its spectrum
+@pytest.mark.parametrize("field,value,code", [("integratorType", 6, _capi.ST_ERR_ARG),
                                               ("dist", b"X", _capi.ST_ERR_UNSUPPORTED),
                                               ("ioutInt", 0.0, _capi.ST_ERR_ARG),
                                               ("numParticles", -1, _capi.ST_ERR_ARG)])
@@ -193,3 +194,22 @@ def test_parse_params_equals_oracle_on_random_files(stlib, oracle, tmp_path):
         assert stlib.st_parse_params(str(path).encode(), ctypes.byref(a)) == 0, path.read_text()
         b = oracle.parse_file(path, derive=False)
         assert bytes(a) == bytes(b), path.read_text()
+
+
+@pytest.mark.parametrize("name", ["probe_spectrum", "probe_spectrum_m"])
+def test_floquet_frequencies_match_reference(stlib, name):
+    """The host library's floquet_diagonalize (the frequencies of the
+    integratorType 6 aggregators) equals the reference build's bit for bit."""
+    import spintrack as st
+    from conftest import GOLDEN
+    lines = (GOLDEN / f"{name}.txt").read_text().splitlines()
+    want = [float.fromhex(x) for x in lines[1].split()[1:]]
+    f, dt = st.floquet_frequencies(st.derive(st.parse_params(GOLDEN / f"{name}.params")))
+    assert list(f) == want[:17] and dt == want[17]
+
+
+def test_spectrum_needs_a_floquet_period(stlib):
+    import spintrack as st
+    opt = st.make_options(integratorType=6, w=0.0, a=5e-6)
+    with pytest.raises(st.SpinTrackError):
+        st.floquet_frequencies(opt)
