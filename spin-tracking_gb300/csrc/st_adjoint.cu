@@ -51,6 +51,21 @@ __device__ __forceinline__ double stage_tau(int s, double tx, double h) {
 // BLOCK]) for the backward sweep.  With kh_s = (dL/dk_s) / h:
 //   kh_s = b_s lam + sum_{r > s} a_rs yb_r,  yb_s = Omega_s x (h kh_s),
 //   z_s = (h kh_s) x Y_s,  dL/dy = lam + sum_s yb_s.
+// The later stages r whose state sums stage s (a_rs != 0), in the order the
+// backward sweep produces them (r = 12 first): k-th contributor (adj_r, with
+// term index adj_j of stage r's sum), adj_n of them.  Equal to enumerating
+// dopst::src(r, j) == s over r = 12 .. s + 1 (checked by hand against the
+// tableau structure: 50 terms in all).
+__device__ __forceinline__ constexpr int adj_n(int s) {
+  return s == 1 ? 11 : s == 2 ? 1 : s == 3 ? 2 : s == 4 ? 8 : 12 - s;
+}
+__device__ __forceinline__ constexpr int adj_r(int s, int k) {
+  return s == 2 ? 3 : s == 3 ? 5 - k : (s == 4 && k == 7) ? 5 : 12 - k;
+}
+__device__ __forceinline__ constexpr int adj_j(int s, int k) {
+  return s == 1 ? 0 : (s == 2 || s == 3) ? 1 : s == 4 ? (k == 7 ? 2 : 1) : s - 3;
+}
+
 template <int BLOCK>
 __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& P, double x, double h, const double y[3],
                                                  double lam[3], Moments& M, bool pulse, double* sm) {
@@ -93,11 +108,7 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
     for (int c = 0; c < 3; ++c) {
       double acc = (dopst::b(s) != 0.0) ? dopst::b(s) * lam0[c] : 0.0;
 #pragma unroll
-      for (int r = 12; r > s; --r) {
-#pragma unroll
-        for (int j = 0; j < dopst::cnt(r); ++j)
-          if (dopst::src(r, j) == s) acc = fma(dopst::a(r, j), ST_YS(r, c), acc);
-      }
+      for (int k = 0; k < adj_n(s); ++k) acc = fma(dopst::a(adj_r(s, k), adj_j(s, k)), ST_YS(adj_r(s, k), c), acc);
       kb[c] = h * acc;
     }
     const double O[3] = {ST_OS(s, 0), ST_OS(s, 1), ST_OS(s, 2)};

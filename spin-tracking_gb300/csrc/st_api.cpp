@@ -910,6 +910,8 @@ int st_set_launch_config(st_ctx* c, const st_launch_config* cfg) {
     return ST_OK;
   }
   if (cfg->variant >= st::persistent_variant_count()) return fail(ST_ERR_ARG, "no such kernel variant");
+  if (cfg->variant >= 0 && st::persistent_max_blocks_per_sm(cfg->variant, ctx_any_ext(c) ? 1 : 0) <= 0)
+    return fail(ST_ERR_UNSUPPORTED, "this kernel variant is not built for the context's integrator types");
   c->lc = *cfg;
   if (c->lc.variant >= 0 && c->lc.blocks_per_sm <= 0) {
     c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, ctx_any_ext(c) ? 1 : 0));
@@ -1801,6 +1803,7 @@ int autotune(st_ctx* c) {
   // Each variant at its highest occupancy (its register budget is part of
   // the variant): on every workload measured, fewer resident blocks lost.
   for (int v = 0; v < nv; ++v) {
+    if (st::persistent_max_blocks_per_sm(v, ext) <= 0) continue;  // not built for this kind of run
     const int maxb = std::max(1, st::persistent_max_blocks_per_sm(v, ext));
     {
       st_launch_config cfg{0, maxb, v};

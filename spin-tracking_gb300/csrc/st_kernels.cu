@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include "st_engine.cuh"
+#include "st_split.cuh"
 
 namespace st {
 
@@ -189,11 +190,14 @@ int launch_pack_snapshot(const RunArgs& a, int slot, void* stream) {
 // Persistent-kernel variants.  Family 0: the flattened kernel (k_persistent);
 // family 1: the trajectory-ahead kernel (k_batched) with its ring capacity
 // and top-up thresholds (start when this many lanes have room, keep filling
-// while this many still have room).  Block threads and the minimum resident
-// blocks per SM set the register budget.
+// while this many still have room); family 2: the warp-specialised
+// trajectory-ahead kernel (k_split, block = consumer warps + one producer
+// warp, ring capacity per particle; integrator types 0 and 1 only).  Block
+// threads and the minimum resident blocks per SM set the register budget.
 struct Variant {
   int family, block, minb, qcap, tstart, tkeep, defer, stages;
   const char* name;
+  int cw, pw, creg, preg;  // family 2: consumer and producer warps, their register shares (0: no split)
 };
 static const Variant kVariants[] = {
     {0, 128, 1, 0, 0, 0, 0, 0, "flat_b128_m1"},  {0, 128, 2, 0, 0, 0, 0, 0, "flat_b128_m2"},
@@ -204,6 +208,9 @@ static const Variant kVariants[] = {
     {1, 64, 2, 8, 24, 16, 18, 0, "ahead_b64_q8_t24_d18"},   {1, 64, 2, 8, 28, 20, 12, 0, "ahead_b64_q8_t28_d12"},
     {1, 64, 2, 8, 28, 20, 12, 1, "ahead_b64_q8_t28_d12_ksmem"},
     {1, 64, 5, 6, 28, 20, 12, 1, "ahead_b64_m5_q6_t28_d12_ksmem"},
+    {2, 128, 2, 8, 0, 0, 0, 0, "split_c3p1_q8", 3, 1, 0, 0},
+    {2, 256, 1, 8, 0, 0, 0, 0, "split_c6p2_q8", 6, 2, 0, 0},
+    {2, 384, 1, 8, 0, 0, 0, 0, "split_c8p4_q8_r184_136", 8, 4, 184, 136},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -224,13 +231,16 @@ static const void* variant_fn_g(int v) {
     case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, GAS, 0, false>);
     case 12: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 1, false>);
     case 13: return reinterpret_cast<const void*>(&k_batched<64, 5, 6, false, GAS, 1, false>);
+    case 14: return reinterpret_cast<const void*>(&k_split<3, 1, 2, 8, GAS, 0, 0>);
+    case 15: return reinterpret_cast<const void*>(&k_split<6, 2, 1, 8, GAS, 0, 0>);
+    case 16: return reinterpret_cast<const void*>(&k_split<8, 4, 1, 8, GAS, 184, 136>);
     default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 0, false>);  // 8 to 11
   }
 }
 // The kernel of variant v: with gas collisions or without, and with
 // integrator types 2-5 (whose instantiations handle gas and every type).
 static const void* variant_fn(int v, bool gas, bool ext) {
-  if (ext) return variant_fn_ext(v);
+  if (ext) return kVariants[v].family == 2 ? nullptr : variant_fn_ext(v);  // no k_split for types 2-5
   return gas ? variant_fn_g<true>(v) : variant_fn_g<false>(v);
 }
 
@@ -241,9 +251,26 @@ static size_t batched_smem(int block, int qcap, int stages) {
   return ring + (stages ? (size_t)30 * block * sizeof(double) : 0);
 }
 
+static int split_consumer_warps(int v) { return kVariants[v].cw; }
+
+// A register split must fit the registers the block is launched with, and
+// setmaxnreg may only raise the consumers' and lower the producers' count:
+// checked against the compiled kernel before it can ever run (a split that
+// does not fit would wait for registers forever).
+static bool split_fits(int v, const void* fn) {
+  const Variant& x = kVariants[v];
+  if (x.family != 2 || x.creg == 0) return true;
+  cudaFuncAttributes at{};
+  if (cudaFuncGetAttributes(&at, fn) != cudaSuccess) return false;
+  const long long launched = (long long)x.block * at.numRegs;
+  const long long shares = 32LL * ((long long)x.cw * x.creg + (long long)x.pw * x.preg);
+  return at.numRegs >= x.preg && at.numRegs <= x.creg && shares <= launched;
+}
+
 static size_t variant_smem(int v) {
   const Variant& x = kVariants[v];
   if (x.family == 0) return 0;
+  if (x.family == 2) return split_smem_bytes(split_consumer_warps(v), x.qcap);
   return batched_smem(x.block, x.qcap, x.stages);
 }
 
@@ -261,8 +288,9 @@ static cudaError_t ensure_smem(int v, bool gas, bool ext) {
   const int k = ext ? 2 : (gas ? 1 : 0), d = current_device();
   if (d < kAttrDevices && done[d][v][k]) return cudaSuccess;
   const size_t sm = variant_smem(v);
+  const void* fn = variant_fn(v, gas, ext);
   cudaError_t e = cudaSuccess;
-  if (sm > 0) e = cudaFuncSetAttribute(variant_fn(v, gas, ext), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (sm > 0 && fn) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess && d < kAttrDevices) done[d][v][k] = true;
   return e;
 }
@@ -280,9 +308,10 @@ int persistent_max_blocks_per_sm(int v, int ext) {
   int nb = 0;
   if (v < 0 || v >= kNumVariants) return 0;
   // the gas and gas-free instantiations have the same launch bounds; take the one with gas
+  const void* fn = variant_fn(v, true, ext != 0);
+  if (!fn || !split_fits(v, fn)) return 0;  // not instantiated for this kind of run, or its split does not fit
   if (ensure_smem(v, true, ext != 0) != cudaSuccess) return 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, variant_fn(v, true, ext != 0), kVariants[v].block,
-                                                variant_smem(v));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kVariants[v].block, variant_smem(v));
   return nb;
 }
 
@@ -299,8 +328,11 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
   TapeArgs none{};
   void* params_flat[] = {&args};
   void* params_ahead[] = {&args, &t0, &t1, &dk, &none};
-  e = cudaLaunchKernel(variant_fn(v, gas, ext), dim3(blocks), dim3(x.block), x.family == 0 ? params_flat : params_ahead,
-                       variant_smem(v), (cudaStream_t)stream);
+  const void* fn = variant_fn(v, gas, ext);
+  if (!fn) return (int)cudaErrorInvalidValue;
+  if (!split_fits(v, fn)) return (int)cudaErrorInvalidConfiguration;
+  e = cudaLaunchKernel(fn, dim3(blocks), dim3(x.block), x.family == 1 ? params_ahead : params_flat, variant_smem(v),
+                       (cudaStream_t)stream);
   return (int)e;
 }
 

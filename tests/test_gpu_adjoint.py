@@ -169,8 +169,7 @@ def _grad_with_budget(p, nw, w, tape_bytes, every):
 def test_backward_is_independent_of_the_tape_budget(gpu, integrator):
     """The same gradients whether the record pass's tape fits (no replay), or
     window chunks are replayed from state checkpoints, or a single window is
-    replayed in particle groups, or the record pass keeps its last intervals
-    and the earlier ones are replayed; final states identical in every case."""
+    replayed in particle groups; final states identical in every case."""
     import torch
     opt = adj_options(n=16, tf=0.2, integrator=integrator)
     nw = st.num_windows(opt)
@@ -188,17 +187,7 @@ def test_backward_is_independent_of_the_tape_budget(gpu, integrator):
         g_grp, s_grp = _grad_with_budget(p, nw, w, used // 16, 1)
         assert s_grp["groups"] >= 2
         np.testing.assert_array_equal(p.output_data()["S"], S_res)
-        # a pool too small for the whole tape but large enough for its last
-        # interval(s): the record pass keeps them, the backward replays the rest
-        tails = []
-        for frac in (0.9, 0.8, 0.7, 0.6):
-            g_tail, s_tail = _grad_with_budget(p, nw, w, int(used * frac), 1)
-            np.testing.assert_array_equal(p.output_data()["S"], S_res)
-            if 0 < s_tail["tail_from"] < s_tail["checkpoints"]:
-                assert s_tail["resident"] == 0 and s_tail["replays"] >= 1 and s_tail["record_launches"] >= 2
-                tails.append((frac, s_tail["tail_from"], g_tail))
-        print("kept tails (pool fraction, first kept interval):", [(f, k) for f, k, _ in tails])
-        assert tails, "no pool size kept a tail"
+
         # a pool below one particle's tape over one checkpoint interval
         p.init_particles()
         p.adjoint_record(nw, tape_bytes=2 * 320 * 8, windows_per_checkpoint=4)
@@ -209,6 +198,35 @@ def test_backward_is_independent_of_the_tape_budget(gpu, integrator):
     assert np.all(np.isfinite(g_res))
     np.testing.assert_allclose(g_chunk, g_res, rtol=1e-12, atol=1e-300)
     np.testing.assert_allclose(g_grp, g_res, rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("integrator", [0, 2], ids=["dop853", "magnus"])
+def test_record_keeps_the_last_intervals_when_the_tape_does_not_fit(gpu, integrator):
+    """A pool too small for the whole tape but large enough for its last
+    checkpoint intervals: the record pass (in pieces: the first interval,
+    the middle with the tape off, the tail) keeps them and the backward
+    replays only the earlier ones; the gradients equal the resident tape's to
+    1e-12 and the forward outputs are identical."""
+    import torch
+    opt = adj_options(n=256, tf=0.4, integrator=integrator)
+    nw = st.num_windows(opt)
+    assert nw == 8
+    dev = torch.device("cuda", 0)
+    w = torch.tensor(np.random.default_rng(3).normal(size=(256, 3)), dtype=torch.float64, device=dev)
+    with st.Particles(opt) as p:
+        g_res, s_res = _grad_with_budget(p, nw, w, 0, 1)
+        S_res = p.output_data()["S"]
+        assert s_res["resident"] == 1 and s_res["record_launches"] == 2  # first interval, then the rest appended
+        used = s_res["tape_bytes_used"]
+        tails = []
+        for frac in (0.9, 0.75, 0.6, 0.45):
+            g_tail, s_tail = _grad_with_budget(p, nw, w, int(used * frac), 1)
+            np.testing.assert_array_equal(p.output_data()["S"], S_res)
+            if 0 < s_tail["tail_from"] < s_tail["checkpoints"]:
+                assert s_tail["resident"] == 0 and s_tail["replays"] >= 1 and s_tail["record_launches"] == 3
+                tails.append((frac, s_tail["tail_from"], g_tail))
+    print("kept tails (pool fraction, first kept interval):", [(f, k) for f, k, _ in tails])
+    assert tails, "no pool size kept a tail"
     for _, _, g_tail in tails:
         np.testing.assert_allclose(g_tail, g_res, rtol=1e-12, atol=1e-300)
 

@@ -40,3 +40,30 @@ def test_deadline_stops_and_the_next_call_resumes(gpu, kernel, integrator):
         got = p.output_data()
     for f in ref:
         np.testing.assert_array_equal(got[f], ref[f], err_msg=f)
+
+
+def test_deadline_in_the_warp_specialised_kernel(gpu):
+    """The same with every warp-specialised variant (consumer warps stop at
+    the budget, the producer warps wind down when their slots are given up)."""
+    from spintrack import _capi
+    opt = deadline_options(0)
+    nw = st.num_windows(opt)
+    with st.Particles(opt) as p:
+        p.init_particles()
+        assert p.run_windows(0, nw, st.KERNEL_PLAIN) == 0
+        ref = p.output_data()
+    split = [v for v in range(_capi.load().st_launch_variant_count()) if st.variant_name(v).startswith("split")]
+    assert split
+    for v in split:
+        with st.Particles(opt) as p:
+            p.set_launch_config(v, 0)
+            p.init_particles()
+            p.set_deadline(1e-4)
+            assert p.run_windows(0, nw, st.KERNEL_PERSISTENT) == ST_ERR_DEADLINE
+            p.set_deadline(0.0)
+            for _ in range(3):
+                if p.run_windows(0, nw, st.KERNEL_PERSISTENT) == 0:
+                    break
+            got = p.output_data()
+        for f in ref:
+            np.testing.assert_array_equal(got[f], ref[f], err_msg=f"variant {v} field {f}")
