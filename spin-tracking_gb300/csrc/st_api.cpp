@@ -304,11 +304,21 @@ int ctx_alloc(st_ctx* c) {
 // the fourth/fifth-order types weighted 2000x (at rtol 1e-12 RK45 takes ~4400x
 // the attempts of DOP853, each ~0.4x the work).
 // Some set integrates with type 2-5: the runs take the EXT kernels.
+bool ctx_any_rk45(const st_ctx* c) {
+  for (const auto& P : c->sets_h)
+    if (P.integrator == 1) return true;
+  return false;
+}
+// Which persistent-kernel instantiations a context's runs need: bit 0 some set
+// has type 2-5, bit 1 some set has RK45.
+int ctx_kind(const st_ctx* c);
+
 bool ctx_any_ext(const st_ctx* c) {
   for (const auto& P : c->sets_h)
     if (P.integrator >= 2 && P.integrator <= 5) return true;
   return false;
 }
+int ctx_kind(const st_ctx* c) { return (ctx_any_ext(c) ? 1 : 0) | (ctx_any_rk45(c) ? 2 : 0); }
 
 int order_group(int it) {
   switch (it) {
@@ -361,6 +371,7 @@ st::RunArgs make_args(st_ctx* c, int w_begin, int w_end, void* snap) {
   a.count_work = 1;
   a.any_gas = 0;
   a.any_ext = ctx_any_ext(c) ? 1 : 0;
+  a.any_rk45 = ctx_any_rk45(c) ? 1 : 0;
   for (const auto& P : c->sets_h) a.any_gas |= P.gas ? 1 : 0;
   return a;
 }
@@ -910,11 +921,11 @@ int st_set_launch_config(st_ctx* c, const st_launch_config* cfg) {
     return ST_OK;
   }
   if (cfg->variant >= st::persistent_variant_count()) return fail(ST_ERR_ARG, "no such kernel variant");
-  if (cfg->variant >= 0 && st::persistent_max_blocks_per_sm(cfg->variant, ctx_any_ext(c) ? 1 : 0) <= 0)
+  if (cfg->variant >= 0 && st::persistent_max_blocks_per_sm(cfg->variant, ctx_kind(c)) <= 0)
     return fail(ST_ERR_UNSUPPORTED, "this kernel variant is not built for the context's integrator types");
   c->lc = *cfg;
   if (c->lc.variant >= 0 && c->lc.blocks_per_sm <= 0) {
-    c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, ctx_any_ext(c) ? 1 : 0));
+    c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, ctx_kind(c)));
   }
   return ST_OK;
 }
@@ -1765,7 +1776,7 @@ int autotune(st_ctx* c) {
     const int it = P.integrator;
     key.ntypes_mask |= it == 0 ? 1 : it == 1 ? 2 : (it >= 2 && it <= 5) ? (8 << (it - 2)) : 4;
   }
-  const int ext = ctx_any_ext(c) ? 1 : 0;
+  const int ext = ctx_kind(c);
   while ((int64_t(1) << key.log2n) < c->n) ++key.log2n;
   {
     std::lock_guard<std::mutex> lock(tune_mutex());

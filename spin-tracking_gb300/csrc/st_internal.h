@@ -100,6 +100,7 @@ struct RunArgs {
   int count_work;                 // accumulate attempt counters
   int any_gas;                    // some set has gas collisions (else gas-free kernels may run)
   int any_ext;                    // some set integrates with type 2-5 (the EXT kernels must run)
+  int any_rk45;                   // some set integrates with RK45 (type 1)
 };
 
 // Discrete adjoint (st_adjoint.cu): gradient of L(S_final) with respect to
@@ -202,7 +203,8 @@ int persistent_variant_count();
 // Host helpers shared across the library's translation units.
 int build_set_params(const st_options& o, int64_t first, SetParams* P);
 int set_last_error(int code, const char* msg);
-int persistent_max_blocks_per_sm(int variant, int ext);  // ext: the integrator type 2-5 kernel
+// kind: bit 0 some set has type 2-5 (the EXT kernels), bit 1 some set has RK45
+int persistent_max_blocks_per_sm(int variant, int kind);
 int persistent_prepare(int variant);
 int persistent_variant_block(int variant);
 const char* persistent_variant_name(int variant);

@@ -25,6 +25,7 @@
 
 #include "st_engine.cuh"
 #include "st_split.cuh"
+#include "st_tpp.cuh"
 
 namespace st {
 
@@ -192,8 +193,10 @@ int launch_pack_snapshot(const RunArgs& a, int slot, void* stream) {
 // and top-up thresholds (start when this many lanes have room, keep filling
 // while this many still have room); family 2: the warp-specialised
 // trajectory-ahead kernel (k_split, block = consumer warps + one producer
-// warp, ring capacity per particle; integrator types 0 and 1 only).  Block
-// threads and the minimum resident blocks per SM set the register budget.
+// warp, ring capacity per particle; integrator types 0 and 1 only); family 3:
+// three lanes per particle (k_tpp3, the flattened loop shape; types 0 and 1,
+// the linear grad hook and the z cosine pulse).  Block threads and the minimum
+// resident blocks per SM set the register budget.
 struct Variant {
   int family, block, minb, qcap, tstart, tkeep, defer, stages;
   const char* name;
@@ -211,6 +214,7 @@ static const Variant kVariants[] = {
     {2, 128, 2, 8, 0, 0, 0, 0, "split_c3p1_q8", 3, 1, 0, 0},
     {2, 256, 1, 8, 0, 0, 0, 0, "split_c6p2_q8", 6, 2, 0, 0},
     {2, 384, 1, 8, 0, 0, 0, 0, "split_c8p4_q8_r184_136", 8, 4, 184, 136},
+    {3, 128, 2, 0, 0, 0, 0, 0, "tpp3_b128_m2"},    {3, 128, 3, 0, 0, 0, 0, 0, "tpp3_b128_m3"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -234,13 +238,22 @@ static const void* variant_fn_g(int v) {
     case 14: return reinterpret_cast<const void*>(&k_split<3, 1, 2, 8, GAS, 0, 0>);
     case 15: return reinterpret_cast<const void*>(&k_split<6, 2, 1, 8, GAS, 0, 0>);
     case 16: return reinterpret_cast<const void*>(&k_split<8, 4, 1, 8, GAS, 184, 136>);
+#if ST_GRAD_IS_LINEAR && ST_PULSE_IS_Z_COS
+    case 17: return reinterpret_cast<const void*>(&k_tpp3<128, 2>);
+    case 18: return reinterpret_cast<const void*>(&k_tpp3<128, 3>);
+#else
+    case 17:
+    case 18: return nullptr;  // the three-lane step assumes the default field hooks
+#endif
     default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 0, false>);  // 8 to 11
   }
 }
 // The kernel of variant v: with gas collisions or without, and with
 // integrator types 2-5 (whose instantiations handle gas and every type).
-static const void* variant_fn(int v, bool gas, bool ext) {
-  if (ext) return kVariants[v].family == 2 ? nullptr : variant_fn_ext(v);  // no k_split for types 2-5
+// kind: bit 0 some set has type 2-5, bit 1 some set has RK45.
+static const void* variant_fn(int v, bool gas, int kind) {
+  if (kind & 1) return kVariants[v].family >= 2 ? nullptr : variant_fn_ext(v);  // no k_split, k_tpp3 for types 2-5
+  if ((kind & 2) && kVariants[v].family == 3) return nullptr;                  // k_tpp3 integrates DOP853 only
   return gas ? variant_fn_g<true>(v) : variant_fn_g<false>(v);
 }
 
@@ -269,7 +282,7 @@ static bool split_fits(int v, const void* fn) {
 
 static size_t variant_smem(int v) {
   const Variant& x = kVariants[v];
-  if (x.family == 0) return 0;
+  if (x.family == 0 || x.family == 3) return 0;
   if (x.family == 2) return split_smem_bytes(split_consumer_warps(v), x.qcap);
   return batched_smem(x.block, x.qcap, x.stages);
 }
@@ -283,12 +296,13 @@ static int current_device() {
 }
 
 // Opt the kernels that need more than 48 KiB of dynamic shared memory in, once per device.
-static cudaError_t ensure_smem(int v, bool gas, bool ext) {
+static cudaError_t ensure_smem(int v, bool gas, int kind) {
+  const bool ext = (kind & 1) != 0;
   static bool done[kAttrDevices][kNumVariants][3] = {};
   const int k = ext ? 2 : (gas ? 1 : 0), d = current_device();
   if (d < kAttrDevices && done[d][v][k]) return cudaSuccess;
   const size_t sm = variant_smem(v);
-  const void* fn = variant_fn(v, gas, ext);
+  const void* fn = variant_fn(v, gas, kind);
   cudaError_t e = cudaSuccess;
   if (sm > 0 && fn) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess && d < kAttrDevices) done[d][v][k] = true;
@@ -298,19 +312,19 @@ static cudaError_t ensure_smem(int v, bool gas, bool ext) {
 // Function attributes of a variant's kernels, set before any graph capture.
 int persistent_prepare(int v) {
   if (v < 0 || v >= kNumVariants) return (int)cudaErrorInvalidValue;
-  cudaError_t e = ensure_smem(v, true, false);
-  if (e == cudaSuccess) e = ensure_smem(v, false, false);
-  if (e == cudaSuccess) e = ensure_smem(v, true, true);
+  cudaError_t e = ensure_smem(v, true, 0);
+  if (e == cudaSuccess) e = ensure_smem(v, false, 0);
+  if (e == cudaSuccess) e = ensure_smem(v, true, 1);
   return (int)e;
 }
 
-int persistent_max_blocks_per_sm(int v, int ext) {
+int persistent_max_blocks_per_sm(int v, int kind) {
   int nb = 0;
   if (v < 0 || v >= kNumVariants) return 0;
   // the gas and gas-free instantiations have the same launch bounds; take the one with gas
-  const void* fn = variant_fn(v, true, ext != 0);
+  const void* fn = variant_fn(v, true, kind);
   if (!fn || !split_fits(v, fn)) return 0;  // not instantiated for this kind of run, or its split does not fit
-  if (ensure_smem(v, true, ext != 0) != cudaSuccess) return 0;
+  if (ensure_smem(v, true, kind) != cudaSuccess) return 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kVariants[v].block, variant_smem(v));
   return nb;
 }
@@ -320,15 +334,16 @@ int launch_persistent(const RunArgs& a, int v, int blocks, int block, void* stre
   if (v < 0 || v >= kNumVariants) return (int)cudaErrorInvalidValue;
   (void)block;
   const Variant& x = kVariants[v];
-  const bool gas = a.any_gas != 0, ext = a.any_ext != 0;
-  cudaError_t e = ensure_smem(v, gas, ext);
+  const bool gas = a.any_gas != 0;
+  const int kind = (a.any_ext ? 1 : 0) | (a.any_rk45 ? 2 : 0);
+  cudaError_t e = ensure_smem(v, gas, kind);
   if (e != cudaSuccess) return (int)e;
   RunArgs args = a;
   int t0 = x.tstart, t1 = x.tkeep, dk = x.defer;
   TapeArgs none{};
   void* params_flat[] = {&args};
   void* params_ahead[] = {&args, &t0, &t1, &dk, &none};
-  const void* fn = variant_fn(v, gas, ext);
+  const void* fn = variant_fn(v, gas, kind);
   if (!fn) return (int)cudaErrorInvalidValue;
   if (!split_fits(v, fn)) return (int)cudaErrorInvalidConfiguration;
   e = cudaLaunchKernel(fn, dim3(blocks), dim3(x.block), x.family == 1 ? params_ahead : params_flat, variant_smem(v),

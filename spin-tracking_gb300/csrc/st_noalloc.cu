@@ -204,7 +204,11 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
   a.count_work = 1;
   a.any_gas = 1;  // the caller's sets are not inspected on the host: the kernel with gas handles any set
   a.any_ext = 0;
-  for (int k = 0; k < nsets; ++k) a.any_ext |= (sets[k].integratorType >= 2 && sets[k].integratorType <= 5) ? 1 : 0;
+  a.any_rk45 = 0;
+  for (int k = 0; k < nsets; ++k) {
+    a.any_ext |= (sets[k].integratorType >= 2 && sets[k].integratorType <= 5) ? 1 : 0;
+    a.any_rk45 |= sets[k].integratorType == 1 ? 1 : 0;
+  }
   if (int pe = launch_prepare_sets(params, nsets, st_)) return set_last_error(ST_ERR_CUDA, cudaGetErrorString((cudaError_t)pe));
   if (n > 0) {
     k_noalloc_sets<<<(unsigned)((n + 255) / 256), 256, 0, st_>>>(a.s, params, nsets);
@@ -212,7 +216,7 @@ extern "C" int st_run_noalloc(const st_options* sets, int nsets, void* state, si
     if (e != cudaSuccess) return set_last_error(ST_ERR_CUDA, cudaGetErrorString(e));
     // flat_b128_m2 (the flattened persistent kernel) at its full occupancy; the
     // occupancy query and the shared-memory attribute allocate nothing
-    const int per_sm = persistent_max_blocks_per_sm(kNoAllocVariant, a.any_ext);
+    const int per_sm = persistent_max_blocks_per_sm(kNoAllocVariant, a.any_ext | (a.any_rk45 << 1));
     if (per_sm < 1) return set_last_error(ST_ERR_CUDA, "st_run_noalloc: the persistent kernel cannot be resident");
     int le = launch_init(a, 256, st_);
     if (!le) le = launch_persistent(a, kNoAllocVariant, sms * per_sm, 0, st_);

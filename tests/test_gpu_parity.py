@@ -91,9 +91,10 @@ def test_run_until_matches_window_driver(gpu):
 
 @pytest.mark.parametrize("case", ["m04_gas", "c_gas", "m42_diffuse", "nmax", "rk45", "traj", "pulse"])
 def test_every_persistent_variant_matches_plain(gpu, case):
-    """Every launch variant of the batched engine (the flattened kernel and the
-    trajectory-ahead kernel with each ring size and top-up rule) runs the same
-    device arithmetic as the plain kernel: outputs must be identical."""
+    """Every launch variant of the batched engine (the flattened kernel, the
+    trajectory-ahead kernel with each ring size and top-up rule, its
+    warp-specialised form and the three-lanes-per-particle kernel) runs the
+    same device arithmetic as the plain kernel: outputs must be identical."""
     from spintrack import _capi
     opt = st.derive(st.parse_params(GOLDEN / f"{case}.params"))
     nwin = st.num_windows(opt)
@@ -103,6 +104,10 @@ def test_every_persistent_variant_matches_plain(gpu, case):
         ref = p.output_data()
     for v in range(_capi.load().st_launch_variant_count()):
         with st.Particles(opt) as p:
+            if st.variant_name(v).startswith("tpp3") and opt.integratorType == 1:
+                with pytest.raises(st.SpinTrackError):  # the three-lane step is DOP853's
+                    p.set_launch_config(v, 0)
+                continue
             p.set_launch_config(v, 0)
             p.init_particles()
             p.run_windows(0, nwin, st.KERNEL_PERSISTENT)
