@@ -30,6 +30,8 @@
 //                                     sanity_check (src/particle.cpp:121-444)
 //                                     with tf = opt.tf; prints per segment
 //                                     coll_type wall_hit dt t pos v next_gas
+//   ref_probe sizes PARAMS            sizeof options, coords, rngState,
+//                                     SpectrumAggregator, floquetDiagonalization
 //   ref_probe spectrum PARAMS ax ay az wx wy wz
 //                                     integratorType 6 (noise amplitudes a and
 //                                     frequencies w set, the params file has no
@@ -147,6 +149,12 @@ int main(int argc, char** argv) {
         }
       }
     }
+    return 0;
+  }
+  if (!std::strcmp(cmd, "sizes")) {  // the struct sizes a launcher of the GPU kernels lays out
+    std::printf("options %zu coords %zu rngState %zu SpectrumAggregator %zu floquetDiagonalization %zu\n",
+                sizeof(options), sizeof(coords), sizeof(rngState), sizeof(SpectrumAggregator),
+                sizeof(floquetDiagonalization));
     return 0;
   }
   if (!std::strcmp(cmd, "spectrum")) {

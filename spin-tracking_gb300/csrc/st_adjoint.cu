@@ -51,21 +51,6 @@ __device__ __forceinline__ double stage_tau(int s, double tx, double h) {
 // BLOCK]) for the backward sweep.  With kh_s = (dL/dk_s) / h:
 //   kh_s = b_s lam + sum_{r > s} a_rs yb_r,  yb_s = Omega_s x (h kh_s),
 //   z_s = (h kh_s) x Y_s,  dL/dy = lam + sum_s yb_s.
-// The later stages r whose state sums stage s (a_rs != 0), in the order the
-// backward sweep produces them (r = 12 first): k-th contributor (adj_r, with
-// term index adj_j of stage r's sum), adj_n of them.  Equal to enumerating
-// dopst::src(r, j) == s over r = 12 .. s + 1 (checked by hand against the
-// tableau structure: 50 terms in all).
-__device__ __forceinline__ constexpr int adj_n(int s) {
-  return s == 1 ? 11 : s == 2 ? 1 : s == 3 ? 2 : s == 4 ? 8 : 12 - s;
-}
-__device__ __forceinline__ constexpr int adj_r(int s, int k) {
-  return s == 2 ? 3 : s == 3 ? 5 - k : (s == 4 && k == 7) ? 5 : 12 - k;
-}
-__device__ __forceinline__ constexpr int adj_j(int s, int k) {
-  return s == 1 ? 0 : (s == 2 || s == 3) ? 1 : s == 4 ? (k == 7 ? 2 : 1) : s - 3;
-}
-
 template <int BLOCK>
 __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& P, double x, double h, const double y[3],
                                                  double lam[3], Moments& M, bool pulse, double* sm) {
@@ -96,29 +81,20 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
     ST_OS(s, 2) = O[2];
     if (s < 12) bloch(Y[0], Y[1], Y[2], O[0], O[1], O[2], K[s - 1][0], K[s - 1][1], K[s - 1][2]);
   }
-  // ---- backward sweep, stage 12 first.  kh_s is gathered when stage s is
-  // reached, from the yb_r of the later stages (r = 12 first, the order in
-  // which they are produced), which replace their stage states in shared
-  // memory once read: no array of twelve accumulators stays live.
-  const double lam0[3] = {lam[0], lam[1], lam[2]};
+  // ---- backward sweep, stage 12 first
+  double kh[12][3];
+#pragma unroll
+  for (int s = 1; s <= 12; ++s)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) kh[s - 1][c] = (dopst::b(s) != 0.0) ? dopst::b(s) * lam[c] : 0.0;
 #pragma unroll
   for (int s = 12; s >= 1; --s) {
-    double kb[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      double acc = (dopst::b(s) != 0.0) ? dopst::b(s) * lam0[c] : 0.0;
-#pragma unroll
-      for (int k = 0; k < adj_n(s); ++k) acc = fma(dopst::a(adj_r(s, k), adj_j(s, k)), ST_YS(adj_r(s, k), c), acc);
-      kb[c] = h * acc;
-    }
+    const double kb[3] = {h * kh[s - 1][0], h * kh[s - 1][1], h * kh[s - 1][2]};
     const double O[3] = {ST_OS(s, 0), ST_OS(s, 1), ST_OS(s, 2)};
     const double Y[3] = {ST_YS(s, 0), ST_YS(s, 1), ST_YS(s, 2)};
     double yb[3], z[3];
     cross3(O, kb, yb);  // dL/dY_s
     cross3(kb, Y, z);   // dL/dOmega_s
-    ST_YS(s, 0) = yb[0];
-    ST_YS(s, 1) = yb[1];
-    ST_YS(s, 2) = yb[2];
     const double tau = stage_tau(s, tx, h);
     const double tau2 = tau * tau;
 #pragma unroll
@@ -134,6 +110,12 @@ __device__ __forceinline__ void dop_step_adjoint(const Seg& g, const SetParams& 
       sincos(P.w * t, &sn, &cs);
       M.ga = fma(P.gamma * cs, z[2], M.ga);
       M.gw = fma(-P.gamma * P.a * t * sn, z[2], M.gw);
+    }
+#pragma unroll
+    for (int j = 0; j < dopst::cnt(s); ++j) {
+      const int l = dopst::src(s, j) - 1;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) kh[l][c] = fma(dopst::a(s, j), yb[c], kh[l][c]);
     }
   }
 #undef ST_YS
@@ -304,8 +286,10 @@ __device__ __forceinline__ void tape_load_seg(const TapeArgs& t, const SetParams
 
 // Lane state machine: fetch a particle from the work order (divergent, once
 // per particle), then one step adjoint per iteration until its tape is
-// exhausted.  Reads lam and adds to grad per particle; the tape's
-// consistency (both chains end together, page indices inside the pool) is
+// exhausted.  Reads lam and grad at the fetch and writes both back when the
+// particle's piece of tape is done, so a backward in pieces (replayed
+// intervals, a kept tail) continues each gradient sum in the order of a
+// backward over the whole tape, bit for bit; the tape's consistency (both chains end together, page indices inside the pool) is
 // checked and a violation sets t.error and abandons the particle.
 // MAGNUS: the tape holds Magnus CFET8 steps (integratorType 2) instead of DOP853 ones.
 template <bool MAGNUS>
@@ -354,7 +338,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
       P = &a.sets[a.s.set[i]];
       tape_load_seg(t, *P, gp, gi, g);
 #pragma unroll
-      for (int q = 0; q < kNumTheta; ++q) gth[q * kAdjBlock] = 0.0;
+      for (int q = 0; q < kNumTheta; ++q) gth[q * kAdjBlock] = t.grad[i * kNumTheta + q];
 #pragma unroll
       for (int c = 0; c < 3; ++c) M.z0[c] = M.z1[c] = M.z2[c] = 0.0;
       M.ga = M.gw = 0.0;
@@ -422,7 +406,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_backward(RunArgs a, TapeArgs 
       t.lam[3 * i + 1] = lam[1];
       t.lam[3 * i + 2] = lam[2];
 #pragma unroll
-      for (int q = 0; q < kNumTheta; ++q) t.grad[i * kNumTheta + q] += gth[q * kAdjBlock];
+      for (int q = 0; q < kNumTheta; ++q) t.grad[i * kNumTheta + q] = gth[q * kAdjBlock];
       active = false;
     }
   }

@@ -196,8 +196,8 @@ def test_backward_is_independent_of_the_tape_budget(gpu, integrator):
         with pytest.raises(st.SpinTrackError):
             p.adjoint_backward(w.data_ptr(), out.data_ptr())
     assert np.all(np.isfinite(g_res))
-    np.testing.assert_allclose(g_chunk, g_res, rtol=1e-12, atol=1e-300)
-    np.testing.assert_allclose(g_grp, g_res, rtol=1e-12, atol=1e-300)
+    np.testing.assert_array_equal(g_chunk, g_res)
+    np.testing.assert_array_equal(g_grp, g_res)
 
 
 @pytest.mark.parametrize("integrator", [0, 2], ids=["dop853", "magnus"])
@@ -205,8 +205,8 @@ def test_record_keeps_the_last_intervals_when_the_tape_does_not_fit(gpu, integra
     """A pool too small for the whole tape but large enough for its last
     checkpoint intervals: the record pass (in pieces: the first interval,
     the middle with the tape off, the tail) keeps them and the backward
-    replays only the earlier ones; the gradients equal the resident tape's to
-    1e-12 and the forward outputs are identical."""
+    replays only the earlier ones; the gradients and the forward outputs equal
+    the resident tape's bit for bit."""
     import torch
     opt = adj_options(n=256, tf=0.4, integrator=integrator)
     nw = st.num_windows(opt)
@@ -228,7 +228,7 @@ def test_record_keeps_the_last_intervals_when_the_tape_does_not_fit(gpu, integra
     print("kept tails (pool fraction, first kept interval):", [(f, k) for f, k, _ in tails])
     assert tails, "no pool size kept a tail"
     for _, _, g_tail in tails:
-        np.testing.assert_allclose(g_tail, g_res, rtol=1e-12, atol=1e-300)
+        np.testing.assert_array_equal(g_tail, g_res)
 
 
 def overshoot_options():
