@@ -147,7 +147,9 @@ int st_synchronize(st_ctx *ctx);
 void *st_get_stream(st_ctx *ctx);
 /* Replace every set's parameters (same particle counts) without reallocating:
  * the device parameter table is re-uploaded; call st_init to restart.  Used
- * for parameter scans.  No counterpart in the reference, which takes options
+ * for parameter scans.  When gas collisions or an integrator type change, an
+ * autotuned launch configuration (or a chosen one that has no kernel for the
+ * new types) is dropped and tuned again at the next run.  No counterpart in the reference, which takes options
  * only at construction (include/particle.h:90). */
 int st_set_params(st_ctx *ctx, const st_options *sets, int nsets);
 /* Bytes of the device parameter table that st_set_params uploads. */

@@ -164,6 +164,7 @@ struct st_ctx {
   bool initialized = false;
   bool window_grid = true;  // particles sit on window boundaries (false after st_run_until off-grid)
   st_launch_config lc{0, 0, -1};
+  bool lc_tuned = false;  // lc came from the autotuner (for the sets it was tuned on)
   int sm_count = 0;
   double deadline_s = 0.0;
   st_counters last{};
@@ -903,6 +904,13 @@ int st_set_params(st_ctx* c, const st_options* sets, int nsets) {
   for (int k = 0; k < nsets; ++k) c->opts[k] = sets[k];
   c->sets_h = P;
   c->adj_recorded = false;  // a recorded tape belongs to the old parameters
+  // A tuned configuration belongs to the old sets' kernels, and a chosen one
+  // may have no instantiation for the new integrator types: tune again.
+  if (kernels_change && c->lc.variant >= 0 &&
+      (c->lc_tuned || st::persistent_max_blocks_per_sm(c->lc.variant, ctx_kind(c)) <= 0)) {
+    c->lc = {0, 0, -1};
+    c->lc_tuned = false;
+  }
   return ST_OK;
 }
 
@@ -924,6 +932,7 @@ int st_set_launch_config(st_ctx* c, const st_launch_config* cfg) {
   if (cfg->variant >= 0 && st::persistent_max_blocks_per_sm(cfg->variant, ctx_kind(c)) <= 0)
     return fail(ST_ERR_UNSUPPORTED, "this kernel variant is not built for the context's integrator types");
   c->lc = *cfg;
+  c->lc_tuned = false;
   if (c->lc.variant >= 0 && c->lc.blocks_per_sm <= 0) {
     c->lc.blocks_per_sm = std::max(1, st::persistent_max_blocks_per_sm(c->lc.variant, ctx_kind(c)));
   }
@@ -1783,6 +1792,7 @@ int autotune(st_ctx* c) {
     auto it = tune_cache().find(key);
     if (it != tune_cache().end()) {
       c->lc = it->second;
+      c->lc_tuned = true;
       return ST_OK;
     }
   }
@@ -1834,6 +1844,7 @@ int autotune(st_ctx* c) {
   }
   st_destroy(s);
   c->lc = best_cfg;
+  c->lc_tuned = true;
   std::lock_guard<std::mutex> lock(tune_mutex());
   tune_cache()[key] = best_cfg;
   return ST_OK;

@@ -237,7 +237,11 @@ static const void* variant_fn_g(int v) {
     case 13: return reinterpret_cast<const void*>(&k_batched<64, 5, 6, false, GAS, 1, false>);
     case 14: return reinterpret_cast<const void*>(&k_split<3, 1, 2, 8, GAS, 0, 0>);
     case 15: return reinterpret_cast<const void*>(&k_split<6, 2, 1, 8, GAS, 0, 0>);
+#if ST_TRAJ_CORRECTLY_ROUNDED
     case 16: return reinterpret_cast<const void*>(&k_split<8, 4, 1, 8, GAS, 184, 136>);
+#else
+    case 16: return nullptr;  // ptxas 13.0 crashes on this instantiation with CUDA's inline log/sin/cos/acos
+#endif
 #if ST_GRAD_IS_LINEAR && ST_PULSE_IS_Z_COS
     case 17: return reinterpret_cast<const void*>(&k_tpp3<128, 2>);
     case 18: return reinterpret_cast<const void*>(&k_tpp3<128, 3>);

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__((CW + PW) * 32, MINB) k_split(RunArgs a) {
   constexpr int NS = CW * 32;
   const SplitSmem m = split_carve(st_smem, NS, QCAP);
   const unsigned FULL = 0xffffffffu;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   if (warp < CW) {  // every slot starts idle with an empty ring
     const int j = threadIdx.x;
     m.si[SI_CTL * NS + j] = kSplitIdle;
