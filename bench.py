@@ -184,6 +184,44 @@ def cpu_sample_rate(tf: float, target_s: float, first: int = 0):
     return n * sim / secs, cores, f"particles [{first}, {first + n}) of the workload, t = 0..{sim:g} s, {secs:.1f} s wall"
 
 
+def reference_gpu_rate(args):
+    """The reference's own CUDA kernels (initParticlesGPU, then runSimulationGPU
+    once per window, built unchanged for sm_103a into the oracle's reference
+    cubin and launched through the driver API) on a sample of the workload: a
+    calibration run of 8,192 particles, then one run sized to about
+    --ref-step-seconds, timed with CUDA events on the launching stream."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+        sys.path.insert(0, str(REPO / "oracle"))
+        sys.path.insert(0, str(REPO / "tests"))
+        import ref_gpu
+        from _oracle import Oracle
+        if not ref_gpu.available():
+            return {"unavailable": "reference cubin not built (it needs the reference sources at build time)"}
+        orc = Oracle()
+        kern = ref_gpu.RefGPU()
+
+        def opts(n):
+            o = apply_fields(orc.default_options(), workload_fields(n, args.tf))
+            orc.L.or_derive(ctypes.byref(o))
+            return o
+        n = 8192
+        secs, _ = kern.run(opts(n), ref_gpu.windows_of(opts(n)))
+        n = int(min(max(n, args.ref_step_seconds / max(secs, 1e-6) * n), args.particles))
+        o = opts(n)
+        nw = ref_gpu.windows_of(o)
+        secs, out = kern.run(o, nw)
+        sim = nw * o.ioutInt
+        return {"value": n * sim / secs, "unit": UNIT, "particles": n, "tf": sim, "seconds": secs,
+                "block": int(o.numPerGPUBlock), "stopped": int((out["fail"] != 0).sum()),
+                "kernels": "the reference's initParticlesGPU + runSimulationGPU per window (src/particle.cpp:450-636), "
+                           "one thread per particle, built unchanged for sm_103a"}
+    except Exception as e:  # the comparison is informative; the CPU line stands without it
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
 # ---------------------------------------------------------------- adjoint
 ADJ_WORKLOAD = ("adjoint: 65,536 particles, MB 4.2 K, specular walls, gravity, gas off, full G ~ N(0,1e-9) T/m, "
                 "E=(0,0,75e5), B0=(3e-6,0,0), DOP853 rtol 1e-12, tf = 1 s (shortened from 50 s), gradients of "
@@ -507,6 +545,8 @@ def run_reference(args, world, rank):
             "sample_per_step": sample,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.skip_reference_gpu:
+        line["reference_gpu"] = reference_gpu_rate(args)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -672,6 +712,8 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--skip-reference-gpu", action="store_true",
+                    help="reference arm: leave out the timing of the reference's own GPU kernels")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=None,
                     help="print the line of one additional configuration instead of the headline line")
     ap.add_argument("--dressing-particles", type=int, default=262144,

@@ -216,7 +216,7 @@ int st_run_noalloc(const st_options *sets, int nsets, void *state, size_t *state
  * st_run_windows does (the trajectory-ahead kernel), and writes the adjoint's
  * tape: every accepted step (y, x, h) and every integrated segment
  * (t0, p0, v0) of every particle, in pages of a device pool of tape_bytes
- * (0 = up to 75% of free device memory).  It also keeps a full-state
+ * (0 = up to 85% of free device memory).  It also keeps a full-state
  * checkpoint every windows_per_checkpoint windows (0 = chosen so the
  * checkpoints take at most 10% of free memory).  A run of four or more
  * checkpoint intervals is recorded in pieces: the first interval's tape

@@ -83,6 +83,18 @@ sv = [dd(mp.sin(j * mp.pi / 256)) for j in range(65)]
 cv = [dd(mp.cos(j * mp.pi / 256)) for j in range(65)]
 out.append("static __device__ const double kSinA[65][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in sv) + "};")
 out.append("static __device__ const double kCosA[65][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in cv) + "};")
+# the fast sin/cos path: pi/1024 in three parts (33 + 33 + 53 bits) and sin, cos of
+# j pi / 1024, j = 0..256
+p1, rest = split(mp.pi / 1024, 33)
+p2, rest = split(rest, 33)
+out.append("// Fast sin/cos path: pi/1024 in three parts (33 + 33 + 53 bits), 1024/pi, and")
+out.append("// sin(j pi / 1024), cos(j pi / 1024), j = 0..256, as hi, lo.")
+out.append("constexpr double kPio10241 = %s, kPio10242 = %s, kPio10243 = %s;" % (h(p1), h(p2), h(float(rest))))
+out.append("constexpr double k1024OverPi = %s;" % h(float(1024 / mp.pi)))
+sv = [dd(mp.sin(j * mp.pi / 1024)) for j in range(257)]
+cv = [dd(mp.cos(j * mp.pi / 1024)) for j in range(257)]
+out.append("static __device__ const double kSinB[257][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in sv) + "};")
+out.append("static __device__ const double kCosB[257][2] = {" + ", ".join("{%s, %s}" % (h(a), h(b)) for a, b in cv) + "};")
 out.append("}  // namespace crm")
 out.append("}  // namespace st")
 print("\n".join(out))

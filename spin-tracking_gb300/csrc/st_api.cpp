@@ -1261,7 +1261,7 @@ int st_adjoint_record(st_ctx* c, int w_end, size_t tape_bytes, int windows_per_c
   size_t want = tape_bytes;
   if (want == 0) {
     ST_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const double cap = 0.75 * (double)free_b;
+    const double cap = 0.85 * (double)free_b;
     const double guess = (double)std::max<int64_t>(c->n, 1) * 16.0 * 1048576.0 + 64.0 * 1048576.0;
     want = (size_t)std::min(cap, guess);
   }

@@ -22,17 +22,19 @@
 //        |t| <= 2^-7, log1p by its Taylor series (fast: terms to t^3 in
 //        double-double, the rest to t^13 in double; accurate: all terms to
 //        t^15 in double-double).
-//   sin/cos: Cody-Waite reduction by pi/2 and by pi/256 with three-part
-//        constants (four-part in the accurate path; exact products for the
-//        arguments used here, |x| < 2^20), table of sin, cos(j pi / 256) in
-//        double-double, Taylor series of the remainder (|s| <= pi/512; fast:
-//        in double, accurate: in double-double to s^15), angle addition.
+//   sin/cos: Cody-Waite reduction by pi/2 with three-part constants (exact
+//        products for the arguments used here, |x| < 2^20), then by pi/1024
+//        (fast path; table of sin, cos(j pi / 1024) in double-double, Taylor
+//        series of the remainder |s| <= pi/2048 in double) or by pi/256 with
+//        four-part constants (accurate path; table at j pi / 256, series to
+//        s^15 in double-double), angle addition.
 //   acos: CUDA's acos as the start y0 and one Newton step on cos(y) = x, whose
 //        residual is formed without cancellation: (1 - x) - 2 sin^2(y0 / 2)
 //        for x >= 1/2 (1 - x is exact there), cos(y0) - x below; the accurate
 //        path repeats the step twice in double-double.  The reflection's sin
-//        and cos of the result reuse the step's evaluation when it rounds to
-//        y0, each with its own rounding test.
+//        and cos of the result are the step's sin and cos of y0 carried to y
+//        to first order (y - y0 is a few ulps), each with its own rounding
+//        test.
 #pragma once
 
 #include "st_crmath_tables.h"
@@ -81,6 +83,17 @@ __device__ __forceinline__ DD dd_mul_d(DD a, double b) {
 }
 __device__ __forceinline__ DD dd_neg(DD a) { return {-a.hi, -a.lo}; }
 __device__ __forceinline__ DD dd_mul_pow2(DD a, double p) { return {a.hi * p, a.lo * p}; }  // exact
+// 1/x to ~2^-22 (the hardware's approximate reciprocal; a host build of this
+// file, for emulation, divides)
+__device__ __forceinline__ double rcp_seed(double x) {
+#ifdef __CUDA_ARCH__
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+#else
+  return 1.0 / x;
+#endif
+}
 // hi = RN(hi + lo) of a normalised pair
 __device__ __forceinline__ double dd_round(DD a) { return __dadd_rn(a.hi, a.lo); }
 
@@ -100,13 +113,14 @@ __device__ __forceinline__ bool rounds_surely(double hi, double lo, double err) 
 
 // Error bounds, relative to the result (and absolute, from the argument
 // reduction of sin and cos), set above the largest errors measured against
-// binary128 on 5 10^6 trajectory arguments per function (log 2^-74.6,
-// sin/cos 2^-83.4, acos 2^-84.0): a fast result is kept only when no rounding
-// boundary lies within the bound, which sends about 2^-17 (log) and 2^-24
+// binary128 on 2 10^7 trajectory arguments per function (log 2^-74.6; sin/cos
+// 2^-70.2, and 2^-69.5 for the reflection's sin and cos carried from y0 to y;
+// the acos Newton step 2^-70.3): a fast result is kept only when no rounding
+// boundary lies within the bound, which sends about 2^-17 (log) and 2^-12
 // (sin, cos, acos) of the calls to the accurate paths.
 constexpr double kLogFastErr = 0x1p-71;
-constexpr double kTrigFastErr = 0x1p-78, kTrigAbsErr = 0x1p-112;
-constexpr double kAcosFastErr = 0x1p-78;
+constexpr double kTrigFastErr = 0x1p-66, kTrigAbsErr = 0x1p-112;
+constexpr double kAcosFastErr = 0x1p-66;
 __device__ __forceinline__ double rel_err(double v, double rel) { return __dmul_ru(fabs(v), rel); }
 
 // ---------------------------------------------------------------- log
@@ -150,12 +164,19 @@ static __device__ __noinline__ double log_accurate(double x) {
   return dd_round(log_assemble(r, dd_mul(r.t, q)));
 }
 
-// Natural logarithm of a positive normal double, correctly rounded (see the
-// file comment); log(1) = 0.
-static __device__ __noinline__ double cr_log(double x) {
+// The fast evaluations are leaf calls that return whether their result is
+// certain; the entry points below (and the trajectory's wrappers) call the
+// accurate paths only when it is not, so the common call makes no nested call.
+
+// Natural logarithm of a positive normal double: the correctly rounded y and
+// true, or false when the fast value's rounding is uncertain; log(1) = 0.
+static __device__ __noinline__ bool cr_log_fast(double x, double& y) {
   const LogReduced r = log_reduce(x);
   const DD t = r.t;
-  if (t.hi == 0.0 && r.e == 0 && r.j >= 31 && r.j <= 32) return 0.0;  // x = 1
+  if (t.hi == 0.0 && r.e == 0 && r.j >= 31 && r.j <= 32) {  // x = 1
+    y = 0.0;
+    return true;
+  }
   // log1p(t) = t - t^2/2 + t^3/3 - t^4/4 + ... + t^13/13
   const double z = t.hi;
   double tail = 1.0 / 13.0;
@@ -176,65 +197,56 @@ static __device__ __noinline__ double cr_log(double x) {
   l = dd_add(l, dd_mul(t3, {kThirdHi, kThirdLo}));
   l = dd_add_d(l, tail);
   const DD s = log_assemble(r, l);
-  if (rounds_surely(s.hi, s.lo, rel_err(s.hi, kLogFastErr))) return s.hi;
-  return log_accurate(x);
+  y = s.hi;
+  return rounds_surely(s.hi, s.lo, rel_err(s.hi, kLogFastErr));
+}
+
+// Natural logarithm of a positive normal double, correctly rounded (see the
+// file comment).
+static __device__ __noinline__ double cr_log(double x) {
+  double y;
+  return cr_log_fast(x, y) ? y : log_accurate(x);
 }
 
 // ---------------------------------------------------------------- sin, cos
 // sin and cos of x, 0 <= |x| < 2^20, as double-double values accurate to
-// ~2^-83 relative (absolute ~2^-120 from the reduction).
+// ~2^-71 relative (absolute ~2^-120 from the reduction): x = k pi/2 + j pi/1024
+// + s, |s| <= pi/2048, the Taylor series of sin s - s and cos s - 1 in double
+// (their rounding is below 2^-72 of the result at that |s|), and the angle
+// addition with the leading product (cos a s for sin, sin a s for cos) exact.
 __device__ __forceinline__ void sincos_dd(double x, DD& sn, DD& cs) {
   // x = k pi/2 + r, r as double-double (k * kPio21 and k * kPio22 are exact)
   const double k = rint(__dmul_rn(x, kTwoOverPi));
   const double r1 = __fma_rn(-k, kPio21, x);
   DD r = two_sum(r1, __dmul_rn(-k, kPio22));
   r = dd_add(r, dd_neg(two_prod(k, kPio23)));
-  // r = j pi/256 + s, |s| <= pi/512 (j * kPio2561 and j * kPio2562 are exact)
-  const double jd = rint(__dmul_rn(r.hi, k256OverPi));
-  DD s = two_sum(__fma_rn(-jd, kPio2561, r.hi), __dmul_rn(-jd, kPio2562));
-  s = dd_add_d(s, r.lo);
-  const double sh = s.hi, sl = __fma_rn(-jd, kPio2563, s.lo);
-  // s = sh + sl.  z = sh^2 exactly.  sin s = sh + sl + p3 + p5 with
-  // p3 = -s^3 / 6 in double-double (s^3 = sh z.hi exactly plus sh z.lo +
-  // 3 z.hi sl) and p5 = s^5 / 5! - s^7 / 7! + s^9 / 9! in double;
-  // cos s - 1 = cph + cpl with cph = -z.hi / 2 exact and cpl = -z.lo / 2 -
-  // sh sl + s^4 / 4! - s^6 / 6! + s^8 / 8!.
-  const DD z = two_prod(sh, sh);
-  DD s3 = two_prod(sh, z.hi);
-  s3.lo = __fma_rn(3.0 * z.hi, sl, __fma_rn(sh, z.lo, s3.lo));
-  const DD p3 = dd_mul(s3, {-kSixthHi, -kSixthLo});
-  const double p5 = __dmul_rn(__dmul_rn(s3.hi, z.hi),
-                             __fma_rn(z.hi, __fma_rn(z.hi, 1.0 / 362880.0, -1.0 / 5040.0), 1.0 / 120.0));
-  const double cph = __dmul_rn(-0.5, z.hi);
-  const double cpl = __fma_rn(__dmul_rn(z.hi, z.hi),
-                              __fma_rn(z.hi, __fma_rn(z.hi, 1.0 / 40320.0, -1.0 / 720.0), 1.0 / 24.0),
-                              __fma_rn(-sh, sl, __dmul_rn(-0.5, z.lo)));
-  // angle addition with the table at a = j pi / 256: the leading terms (the
-  // table value, cos a sh, sin a cph and cos a p3.hi for sin; their
-  // counterparts for cos) summed exactly, the rest (below 2^-34 of the
-  // result) in double
+  // r = j pi/1024 + s (j * kPio10241 and j * kPio10242 are exact, |j| <= 256)
+  const double jd = rint(__dmul_rn(r.hi, k1024OverPi));
+  DD t = two_sum(__fma_rn(-jd, kPio10241, r.hi), __dmul_rn(-jd, kPio10242));
+  t = dd_add_d(t, r.lo);
+  const double sh = t.hi, sl = __fma_rn(-jd, kPio10243, t.lo);
+  // sin s - sh = sl - s^3/6 + s^5/120 - s^7/5040; cos s - 1 = -s^2/2 + s^4/24 - s^6/720
+  const double z = __dmul_rn(sh, sh);
+  const double sp = __dmul_rn(__dmul_rn(sh, z), __fma_rn(z, __fma_rn(z, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0));
+  const double cp = __fma_rn(-sh, sl, __dmul_rn(z, __fma_rn(z, __fma_rn(z, -1.0 / 720.0, 1.0 / 24.0), -0.5)));
+  const double ss = __dadd_rn(sl, sp);
   const int ja = (int)fabs(jd);
-  double sah = kSinA[ja][0], sal = kSinA[ja][1];
+  double sah = kSinB[ja][0], sal = kSinB[ja][1];
   if (jd < 0.0) {
     sah = -sah;
     sal = -sal;
   }
-  const double cah = kCosA[ja][0], cal = kCosA[ja][1];
-  const double rest_s = __dadd_rn(__dadd_rn(sl, p3.lo), p5);  // sin s - sh - p3.hi
-  // sin(a + s) = sin a + cos a (sin s) + sin a (cos s - 1)
-  const DD e1 = two_prod(cah, sh), e2 = two_prod(sah, cph), e3 = two_prod(cah, p3.hi);
-  const DD h1 = two_sum(sah, e1.hi), h2 = two_sum(h1.hi, e2.hi), h3 = two_sum(h2.hi, e3.hi);
-  const double sh3 = __dadd_rn(sh, p3.hi);  // the low table parts multiply sin s to 2^-60
-  double ts = __fma_rn(cah, rest_s, __fma_rn(cal, sh3, __fma_rn(sah, cpl, __fma_rn(sal, cph, sal))));
-  ts = __dadd_rn(ts, __dadd_rn(__dadd_rn(__dadd_rn(e1.lo, e2.lo), e3.lo), __dadd_rn(__dadd_rn(h1.lo, h2.lo), h3.lo)));
-  const DD sr = fast_two_sum(h3.hi, ts);
-  // cos(a + s) = cos a - sin a (sin s) + cos a (cos s - 1)
-  const DD f1 = two_prod(-sah, sh), f2 = two_prod(cah, cph), f3 = two_prod(-sah, p3.hi);
-  const DD g1 = two_sum(cah, f1.hi), g2 = two_sum(g1.hi, f2.hi), g3 = two_sum(g2.hi, f3.hi);
-  double tc = __fma_rn(-sah, rest_s, __fma_rn(-sal, sh3, __fma_rn(cah, cpl, __fma_rn(cal, cph, cal))));
-  tc = __dadd_rn(tc, __dadd_rn(__dadd_rn(__dadd_rn(f1.lo, f2.lo), f3.lo), __dadd_rn(__dadd_rn(g1.lo, g2.lo), g3.lo)));
-  const DD cr = fast_two_sum(g3.hi, tc);
-  // quadrant
+  const double cah = kCosB[ja][0], cal = kCosB[ja][1];
+  // sin(a + s) = sin a + cos a sh + [cos a (sin s - sh) + sin a (cos s - 1)]
+  const DD m = two_prod(cah, sh);
+  const DD hs = two_sum(sah, m.hi);
+  const double ts = __dadd_rn(__dadd_rn(m.lo, sal), __fma_rn(cal, sh, __fma_rn(sah, cp, __dmul_rn(cah, ss))));
+  const DD sr = fast_two_sum(hs.hi, __dadd_rn(hs.lo, ts));
+  // cos(a + s) = cos a - sin a sh + [cos a (cos s - 1) - sin a (sin s - sh)]
+  const DD m2 = two_prod(-sah, sh);
+  const DD hc = two_sum(cah, m2.hi);
+  const double tc = __dadd_rn(__dadd_rn(m2.lo, cal), __fma_rn(-sal, sh, __fma_rn(cah, cp, __dmul_rn(-sah, ss))));
+  const DD cr = fast_two_sum(hc.hi, __dadd_rn(hc.lo, tc));
   const int q = ((int)k) & 3;
   if (q == 0) {
     sn = sr; cs = cr;
@@ -300,13 +312,19 @@ static __device__ __noinline__ void sincos_accurate(double x, double& s, double&
   c = dd_round(cs);
 }
 
-// sin and cos of x, 0 <= |x| < 2^20, each correctly rounded (see the file comment).
-static __device__ __noinline__ void cr_sincos(double x, double& s, double& c) {
+// sin and cos of x, 0 <= |x| < 2^20: the correctly rounded pair and true, or
+// false when the rounding of either is uncertain.
+static __device__ __noinline__ bool cr_sincos_fast(double x, double& s, double& c) {
   DD sn, cs;
   sincos_dd(x, sn, cs);
   s = sn.hi;
   c = cs.hi;
-  if (!(trig_sure(sn) && trig_sure(cs))) sincos_accurate(x, s, c);
+  return trig_sure(sn) && trig_sure(cs);
+}
+
+// sin and cos of x, 0 <= |x| < 2^20, each correctly rounded (see the file comment).
+static __device__ __noinline__ void cr_sincos(double x, double& s, double& c) {
+  if (!cr_sincos_fast(x, s, c)) sincos_accurate(x, s, c);
 }
 
 // ---------------------------------------------------------------- acos
@@ -335,11 +353,61 @@ static __device__ __noinline__ double acos_accurate(double x, DD y) {
   return dd_round(y);
 }
 
+// One Newton step on cos(y) = x from y0 (CUDA's acos, x in [0, 1)): yd as
+// double-double, with the double-double sin and cos of y0.  For x >= 1/2 the
+// residual is (1 - x) - 2 sin^2(y0 / 2) (exact halving, no cancellation).
+__device__ __forceinline__ void acos_newton(double x, double y0, DD& yd, DD& sn, DD& cs) {
+  double g;  // cos(y0) - x
+  if (x >= 0.5) {
+    DD s2, c2;
+    sincos_dd(__dmul_rn(0.5, y0), s2, c2);
+    const DD v = dd_mul_pow2(dd_mul(s2, s2), 2.0);  // 1 - cos(y0)
+    g = dd_round(dd_add_d(dd_neg(v), __dsub_rn(1.0, x)));
+    sn = dd_mul_pow2(dd_mul(s2, c2), 2.0);
+    cs = dd_add_d(dd_neg(v), 1.0);
+  } else {
+    sincos_dd(y0, sn, cs);
+    g = dd_round(dd_add_d(cs, -x));
+  }
+  // the correction g / sin(y0) is a few ulps of y0, so a reciprocal to 2^-44
+  // (hardware seed and one Newton step) leaves it exact to ~2^-96 of y0
+  const double q = dd_round(sn);
+  double r = rcp_seed(q);
+  r = __fma_rn(r, __fma_rn(-q, r, 1.0), r);
+  yd = two_sum(y0, __dmul_rn(g, r));
+}
+// sin and cos of y0 + d from those of y0, for d a few ulps of y0 (exact):
+// sin y0 + d cos y0 and cos y0 - d sin y0, to d^2 / 2 < 2^-100 of the result.
+__device__ __forceinline__ void sincos_shift(double d, DD& sn, DD& cs) {
+  if (d == 0.0) return;
+  const double s0 = sn.hi;
+  sn = dd_add_d(sn, __dmul_rn(d, cs.hi));
+  cs = dd_add_d(cs, __dmul_rn(-d, s0));
+}
+
 // y = acos(x) for x in [0, 1], correctly rounded, with sin(y) and cos(y)
-// correctly rounded too (a cosine-law reflection needs all three).  CUDA's
-// acos gives y0; one Newton step with the double-double sin and cos of y0
-// (of y0 / 2 for x >= 1/2) gives y; when y rounds to y0 (most arguments)
-// those sin and cos are y's, else they are evaluated again.
+// correctly rounded too (a cosine-law reflection needs all three): a Newton
+// step from CUDA's acos, the sin and cos of that y0 carried to y to first
+// order, each value kept when its rounding is certain (Ziv's test) and
+// evaluated by the accurate paths otherwise.  The _fast form returns false
+// instead of taking an accurate path.
+static __device__ __noinline__ bool cr_acos_sincos_fast(double x, double& y, double& sy, double& cy) {
+  const double y0 = acos(x);
+  if (x >= 1.0 || x != x) {  // acos(1) = 0 exactly; NaN passes through
+    y = y0;
+    sy = y0 == 0.0 ? 0.0 : y0;
+    cy = y0 == 0.0 ? 1.0 : y0;
+    return true;
+  }
+  DD yd, sn, cs;
+  acos_newton(x, y0, yd, sn, cs);
+  y = yd.hi;
+  sincos_shift(__dsub_rn(y, y0), sn, cs);
+  sy = sn.hi;
+  cy = cs.hi;
+  return rounds_surely(yd.hi, yd.lo, rel_err(yd.hi, kAcosFastErr)) && trig_sure(sn) && trig_sure(cs);
+}
+
 static __device__ __noinline__ void cr_acos_sincos(double x, double& y, double& sy, double& cy) {
   const double y0 = acos(x);
   if (x >= 1.0 || x != x) {  // acos(1) = 0 exactly; NaN passes through
@@ -348,23 +416,11 @@ static __device__ __noinline__ void cr_acos_sincos(double x, double& y, double& 
     cy = y0 == 0.0 ? 1.0 : y0;
     return;
   }
-  DD sn, cs;  // sin(y0), cos(y0)
-  double g;   // cos(y0) - x
-  if (x >= 0.5) {
-    DD s2, c2;  // of y0 / 2 (exact halving)
-    sincos_dd(__dmul_rn(0.5, y0), s2, c2);
-    const DD v = dd_mul_pow2(dd_mul(s2, s2), 2.0);  // 1 - cos(y0) = 2 sin^2(y0 / 2)
-    g = dd_round(dd_add_d(dd_neg(v), __dsub_rn(1.0, x)));
-    sn = dd_mul_pow2(dd_mul(s2, c2), 2.0);
-    cs = dd_add_d(dd_neg(v), 1.0);
-  } else {
-    sincos_dd(y0, sn, cs);
-    g = dd_round(dd_add_d(cs, -x));
-  }
-  const DD yd = two_sum(y0, __ddiv_rn(g, dd_round(sn)));
+  DD yd, sn, cs;
+  acos_newton(x, y0, yd, sn, cs);
   y = yd.hi;
   if (!rounds_surely(yd.hi, yd.lo, rel_err(yd.hi, kAcosFastErr))) y = acos_accurate(x, yd);
-  if (y != y0) sincos_dd(y, sn, cs);
+  sincos_shift(__dsub_rn(y, y0), sn, cs);
   sy = sn.hi;
   cy = cs.hi;
   if (!(trig_sure(sn) && trig_sure(cs))) sincos_accurate(y, sy, cy);

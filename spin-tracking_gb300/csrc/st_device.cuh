@@ -27,7 +27,8 @@ namespace st {
 // The trajectory's transcendental functions (ST_TRAJ_CORRECTLY_ROUNDED, st_fields.cuh).
 __device__ __forceinline__ double traj_log(double x) {
 #if ST_TRAJ_CORRECTLY_ROUNDED
-  return crm::cr_log(x);
+  double y;
+  return crm::cr_log_fast(x, y) ? y : crm::log_accurate(x);
 #else
   return log(x);
 #endif
@@ -35,7 +36,7 @@ __device__ __forceinline__ double traj_log(double x) {
 // acos(x) and the sin and cos of the result
 __device__ __forceinline__ void traj_acos_sincos(double x, double& y, double& sy, double& cy) {
 #if ST_TRAJ_CORRECTLY_ROUNDED
-  crm::cr_acos_sincos(x, y, sy, cy);
+  if (!crm::cr_acos_sincos_fast(x, y, sy, cy)) crm::cr_acos_sincos(x, y, sy, cy);
 #else
   y = acos(x);
   sy = sin(y);
@@ -44,7 +45,7 @@ __device__ __forceinline__ void traj_acos_sincos(double x, double& y, double& sy
 }
 __device__ __forceinline__ void traj_sincos(double x, double& s, double& c) {
 #if ST_TRAJ_CORRECTLY_ROUNDED
-  crm::cr_sincos(x, s, c);
+  if (!crm::cr_sincos_fast(x, s, c)) crm::sincos_accurate(x, s, c);
 #else
   s = sin(x);
   c = cos(x);
