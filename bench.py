@@ -19,7 +19,9 @@ kernel, snapshots written to a device buffer.
 
 --impl reference times the reference algorithm's CPU implementation on this
 host's cores (the C restatement in oracle/, which reproduces the reference
-build bit for bit) on bounded samples of the same workload.
+build bit for bit) on bounded samples of the same workload; beside it, under
+"reference_gpu", the reference's own CUDA kernels built unchanged for sm_103a
+(when their cubin was built with the reference sources present) on a sample.
 """
 from __future__ import annotations
 
@@ -189,7 +191,9 @@ def reference_gpu_rate(args):
     once per window, built unchanged for sm_103a into the oracle's reference
     cubin and launched through the driver API) on a sample of the workload: a
     calibration run of 8,192 particles, then one run sized to about
-    --ref-step-seconds, timed with CUDA events on the launching stream."""
+    --ref-gpu-seconds (one thread per particle: a sample much larger than the
+    GPU's 38,912 resident threads, so that the last particles do not decide),
+    timed with CUDA events on the launching stream."""
     try:
         import torch
         if not torch.cuda.is_available():
@@ -209,7 +213,7 @@ def reference_gpu_rate(args):
             return o
         n = 8192
         secs, _ = kern.run(opts(n), ref_gpu.windows_of(opts(n)))
-        n = int(min(max(n, args.ref_step_seconds / max(secs, 1e-6) * n), args.particles))
+        n = int(min(max(n, args.ref_gpu_seconds / max(secs, 1e-6) * n), args.particles))
         o = opts(n)
         nw = ref_gpu.windows_of(o)
         secs, out = kern.run(o, nw)
@@ -627,11 +631,14 @@ def run_ours(args, world, rank, local):
                            "nominal GB300 FP64 1.25 TFLOP/s)",
             "work_per_launch": {"dop_attempts": counters["dop_attempts"], "segments": counters["segments"],
                                 "flops": flops, "kernel_ms": kernel_s * 1e3}}
-    # DRAM bytes of one launch, from an ncu capture of the same kernel on 65,536 particles of this
-    # workload (dram__bytes_read + write = 11.67 MB + 0, profiles/k_batched_bench_65k_full.md):
-    # 178 B per particle (its state, read once), scaled to this launch's particles.
-    roof["traffic"] = 178.0 * n
-    roof["traffic_source"] = "ncu capture of 65,536 particles (178 B per particle), scaled to this launch"
+    # DRAM bytes of one launch, from an ncu capture of dram__bytes_read.sum + dram__bytes_write.sum
+    # (one pass) of this kernel on this workload at its full size, 1,048,576 particles and two
+    # windows: 292.98 MB read (the state, once) + 458.02 MB written (the state and a snapshot block
+    # at each window end), 716.2 B per particle per two windows; other sizes scale by particles and
+    # windows (every particle's state and snapshot cross DRAM once per window end).
+    roof["traffic"] = 751.0e6 * (n / 1048576.0) * (nwin / 2.0)
+    roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel on the full "
+                              "workload (1,048,576 particles, 2 windows: 751.0 MB), scaled to this launch")
 
     # ---- plain one-thread-per-particle kernel on the same workload (1 step)
     plain = None
@@ -712,6 +719,8 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-gpu-seconds", type=float, default=30.0,
+                    help="reference arm: target duration of the reference GPU kernels' sample")
     ap.add_argument("--skip-reference-gpu", action="store_true",
                     help="reference arm: leave out the timing of the reference's own GPU kernels")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=None,

@@ -356,17 +356,19 @@ static __device__ __noinline__ double acos_accurate(double x, DD y) {
 // One Newton step on cos(y) = x from y0 (CUDA's acos, x in [0, 1)): yd as
 // double-double, with the double-double sin and cos of y0.  For x >= 1/2 the
 // residual is (1 - x) - 2 sin^2(y0 / 2) (exact halving, no cancellation).
-__device__ __forceinline__ void acos_newton(double x, double y0, DD& yd, DD& sn, DD& cs) {
+// The step takes the sin and cos of acos_newton_arg(x, y0) (y0 / 2 or y0),
+// sa and ca, from its caller.
+__device__ __forceinline__ double acos_newton_arg(double x, double y0) { return x >= 0.5 ? __dmul_rn(0.5, y0) : y0; }
+__device__ __forceinline__ void acos_newton_given(double x, double y0, DD sa, DD ca, DD& yd, DD& sn, DD& cs) {
   double g;  // cos(y0) - x
   if (x >= 0.5) {
-    DD s2, c2;
-    sincos_dd(__dmul_rn(0.5, y0), s2, c2);
-    const DD v = dd_mul_pow2(dd_mul(s2, s2), 2.0);  // 1 - cos(y0)
+    const DD v = dd_mul_pow2(dd_mul(sa, sa), 2.0);  // 1 - cos(y0)
     g = dd_round(dd_add_d(dd_neg(v), __dsub_rn(1.0, x)));
-    sn = dd_mul_pow2(dd_mul(s2, c2), 2.0);
+    sn = dd_mul_pow2(dd_mul(sa, ca), 2.0);
     cs = dd_add_d(dd_neg(v), 1.0);
   } else {
-    sincos_dd(y0, sn, cs);
+    sn = sa;
+    cs = ca;
     g = dd_round(dd_add_d(cs, -x));
   }
   // the correction g / sin(y0) is a few ulps of y0, so a reciprocal to 2^-44
@@ -375,6 +377,11 @@ __device__ __forceinline__ void acos_newton(double x, double y0, DD& yd, DD& sn,
   double r = rcp_seed(q);
   r = __fma_rn(r, __fma_rn(-q, r, 1.0), r);
   yd = two_sum(y0, __dmul_rn(g, r));
+}
+__device__ __forceinline__ void acos_newton(double x, double y0, DD& yd, DD& sn, DD& cs) {
+  DD sa, ca;
+  sincos_dd(acos_newton_arg(x, y0), sa, ca);
+  acos_newton_given(x, y0, sa, ca, yd, sn, cs);
 }
 // sin and cos of y0 + d from those of y0, for d a few ulps of y0 (exact):
 // sin y0 + d cos y0 and cos y0 - d sin y0, to d^2 / 2 < 2^-100 of the result.
@@ -391,8 +398,10 @@ __device__ __forceinline__ void sincos_shift(double d, DD& sn, DD& cs) {
 // order, each value kept when its rounding is certain (Ziv's test) and
 // evaluated by the accurate paths otherwise.  The _fast form returns false
 // instead of taking an accurate path.
-static __device__ __noinline__ bool cr_acos_sincos_fast(double x, double& y, double& sy, double& cy) {
-  const double y0 = acos(x);
+// The fast form from y0 = acos(x) and the sin and cos of acos_newton_arg(x,
+// y0), for callers that evaluate those themselves.
+__device__ __forceinline__ bool acos_sincos_given(double x, double y0, DD sa, DD ca, double& y, double& sy,
+                                                  double& cy) {
   if (x >= 1.0 || x != x) {  // acos(1) = 0 exactly; NaN passes through
     y = y0;
     sy = y0 == 0.0 ? 0.0 : y0;
@@ -400,12 +409,18 @@ static __device__ __noinline__ bool cr_acos_sincos_fast(double x, double& y, dou
     return true;
   }
   DD yd, sn, cs;
-  acos_newton(x, y0, yd, sn, cs);
+  acos_newton_given(x, y0, sa, ca, yd, sn, cs);
   y = yd.hi;
   sincos_shift(__dsub_rn(y, y0), sn, cs);
   sy = sn.hi;
   cy = cs.hi;
   return rounds_surely(yd.hi, yd.lo, rel_err(yd.hi, kAcosFastErr)) && trig_sure(sn) && trig_sure(cs);
+}
+static __device__ __noinline__ bool cr_acos_sincos_fast(double x, double& y, double& sy, double& cy) {
+  const double y0 = acos(x);
+  DD sa{0.0, 0.0}, ca{1.0, 0.0};
+  if (x < 1.0) sincos_dd(acos_newton_arg(x, y0), sa, ca);  // NaN and 1 need none
+  return acos_sincos_given(x, y0, sa, ca, y, sy, cy);
 }
 
 static __device__ __noinline__ void cr_acos_sincos(double x, double& y, double& sy, double& cy) {

@@ -279,11 +279,10 @@ struct DiffuseDefer {
   bool pending;
 };
 
-// New velocity of a cosine-law diffuse reflection off wall w (src/particle.cpp:309-328).
-__device__ __forceinline__ void diffuse_velocity(PState& p, double su, double theta, double speed, char w) {
-  double phi, cp, sp, ct, stt;
-  traj_acos_sincos(su, phi, sp, cp);
-  traj_sincos(theta, stt, ct);
+// New velocity of a cosine-law diffuse reflection off wall w from the sin and
+// cos of phi = acos(sqrt u1) and of theta = 2 pi u2 (src/particle.cpp:309-328).
+__device__ __forceinline__ void diffuse_apply(PState& p, double sp, double cp, double stt, double ct, double speed,
+                                              char w) {
   if (w == 'x') {
     p.vx = xmul(xmul(xmul(-1.0, sgn1(p.vx)), speed), cp);
     p.vy = xmul(xmul(-speed, sp), ct);
@@ -297,6 +296,89 @@ __device__ __forceinline__ void diffuse_velocity(PState& p, double su, double th
     p.vy = xmul(xmul(speed, sp), stt);
     p.vz = xmul(xmul(xmul(-1.0, sgn1(p.vz)), speed), cp);
   }
+}
+
+// New velocity of a cosine-law diffuse reflection off wall w (src/particle.cpp:309-328).
+__device__ __forceinline__ void diffuse_velocity(PState& p, double su, double theta, double speed, char w) {
+  double phi, cp, sp, ct, stt;
+  traj_acos_sincos(su, phi, sp, cp);
+  traj_sincos(theta, stt, ct);
+  diffuse_apply(p, sp, cp, stt, ct, speed, w);
+}
+
+// Position of the k-th set bit of m, counting from 0 (k < popc(m)).
+__device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
+  int p = 0;
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const int c = __popc(m & ((1u << s) - 1u));
+    if (k >= c) {
+      k -= c;
+      m >>= s;
+      p += s;
+    }
+  }
+  return p;
+}
+
+// The deferred diffuse reflections of a warp, lanes `pend`, computed by all
+// 32 lanes together (the warp must be converged).  A reflection needs the sin
+// and cos of two angles: the argument of its acos Newton step and theta.
+// Those 2 popc(pend) evaluations are dealt out one per lane per pass (one pass
+// for up to 16 reflections) instead of two after each other on each pending
+// lane; each pending lane then finishes its own reflection from the shuffled
+// results.  The arithmetic of every evaluation is diffuse_velocity's, so the
+// velocities are the same bit for bit.
+__device__ __forceinline__ void diffuse_velocity_warp(PState& p, DiffuseDefer& dd, unsigned pend, int lane) {
+#if ST_TRAJ_CORRECTLY_ROUNDED
+  const unsigned FULL = 0xffffffffu;
+  const int np = __popc(pend);
+  const bool mine = dd.pending;
+  const double x = dd.su;
+  double y0 = 0.0, arg_a = 0.0;
+  if (mine) {
+    y0 = acos(x);
+    arg_a = x < 1.0 ? crm::acos_newton_arg(x, y0) : 0.0;  // NaN and 1 use none
+  }
+  const int rank = __popc(pend & ((1u << lane) - 1u));
+  crm::DD sa{0.0, 0.0}, ca{1.0, 0.0}, st{0.0, 0.0}, ct{1.0, 0.0};
+  for (int base = 0; base < 2 * np; base += 32) {
+    // job j = base + lane: the Newton argument of pending lane j (j < np) or
+    // the theta of pending lane j - np
+    const int j = base + lane;
+    const int src = nth_set_bit(pend, min(j < np ? j : j - np, np - 1));
+    const double a1 = __shfl_sync(FULL, arg_a, src), a2 = __shfl_sync(FULL, dd.theta, src);
+    crm::DD sn, cs;
+    crm::sincos_dd(j < np ? a1 : a2, sn, cs);
+    // pending lane of rank r takes jobs r and np + r
+    const int ja = rank - base, jb = np + rank - base;
+    const double v0 = __shfl_sync(FULL, sn.hi, ja & 31), v1 = __shfl_sync(FULL, sn.lo, ja & 31);
+    const double v2 = __shfl_sync(FULL, cs.hi, ja & 31), v3 = __shfl_sync(FULL, cs.lo, ja & 31);
+    const double w0 = __shfl_sync(FULL, sn.hi, jb & 31), w1 = __shfl_sync(FULL, sn.lo, jb & 31);
+    const double w2 = __shfl_sync(FULL, cs.hi, jb & 31), w3 = __shfl_sync(FULL, cs.lo, jb & 31);
+    if (ja >= 0 && ja < 32) {
+      sa = {v0, v1};
+      ca = {v2, v3};
+    }
+    if (jb >= 0 && jb < 32) {
+      st = {w0, w1};
+      ct = {w2, w3};
+    }
+  }
+  if (mine) {
+    double phi, sp, cp;
+    if (!crm::acos_sincos_given(x, y0, sa, ca, phi, sp, cp)) crm::cr_acos_sincos(x, phi, sp, cp);
+    double stt = st.hi, ctt = ct.hi;
+    if (!(crm::trig_sure(st) && crm::trig_sure(ct))) crm::sincos_accurate(dd.theta, stt, ctt);
+    diffuse_apply(p, sp, cp, stt, ctt, dd.speed, dd.wall);
+    dd.pending = false;
+  }
+#else
+  if (dd.pending) {
+    diffuse_velocity(p, dd.su, dd.theta, dd.speed, dd.wall);
+    dd.pending = false;
+  }
+#endif
 }
 
 // One trajectory event: calc_next_collision_time, update_position_and_velocity

@@ -574,12 +574,8 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     const unsigned starved_m = __ballot_sync(FULL, starved);
     const unsigned defer_m = __ballot_sync(FULL, dd.pending);
     if (defer_m != 0u &&
-        (__popc(defer_m) >= defer_k || __any_sync(FULL, dd.pending && (starved || qcount <= 1 || mode == B_WEND)))) {
-      if (dd.pending) {
-        diffuse_velocity(tp, dd.su, dd.theta, dd.speed, dd.wall);
-        dd.pending = false;
-      }
-    }
+        (__popc(defer_m) >= defer_k || __any_sync(FULL, dd.pending && (starved || qcount <= 1 || mode == B_WEND))))
+      diffuse_velocity_warp(tp, dd, defer_m, tid & 31);
     bool prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP && !dd.pending;
     unsigned pm = __ballot_sync(FULL, prod);
     if (starved_m != 0u || __popc(pm) >= topup_start) {

@@ -215,6 +215,7 @@ static const Variant kVariants[] = {
     {2, 256, 1, 8, 0, 0, 0, 0, "split_c6p2_q8", 6, 2, 0, 0},
     {2, 384, 1, 8, 0, 0, 0, 0, "split_c8p4_q8_r184_136", 8, 4, 184, 136},
     {3, 128, 2, 0, 0, 0, 0, 0, "tpp3_b128_m2"},    {3, 128, 3, 0, 0, 0, 0, 0, "tpp3_b128_m3"},
+    {1, 128, 1, 6, 16, 12, 16, 0, "ahead_b128_q6_t16_d16"}, {1, 64, 2, 8, 24, 16, 16, 0, "ahead_b64_q8_t24_d16"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -231,7 +232,8 @@ static const void* variant_fn_g(int v) {
     case 3: return reinterpret_cast<const void*>(&k_persistent<64, 4, false>);
     case 4: return reinterpret_cast<const void*>(&k_persistent<256, 1, false>);
     case 5:
-    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, GAS, 0, false>);
+    case 6:
+    case 19: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, GAS, 0, false>);
     case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, GAS, 0, false>);
     case 12: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 1, false>);
     case 13: return reinterpret_cast<const void*>(&k_batched<64, 5, 6, false, GAS, 1, false>);
@@ -249,7 +251,7 @@ static const void* variant_fn_g(int v) {
     case 17:
     case 18: return nullptr;  // the three-lane step assumes the default field hooks
 #endif
-    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 0, false>);  // 8 to 11
+    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 0, false>);  // 8 to 11, 20
   }
 }
 // The kernel of variant v: with gas collisions or without, and with

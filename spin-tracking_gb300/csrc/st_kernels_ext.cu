@@ -17,11 +17,12 @@ const void* variant_fn_ext(int v) {
     case 3: return reinterpret_cast<const void*>(&k_persistent<64, 4, true>);
     case 4: return reinterpret_cast<const void*>(&k_persistent<256, 1, true>);
     case 5:
-    case 6: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, true, 0, true>);
+    case 6:
+    case 19: return reinterpret_cast<const void*>(&k_batched<128, 1, 6, false, true, 0, true>);
     case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, true, 0, true>);
     case 12: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, true, 1, true>);
     case 13: return reinterpret_cast<const void*>(&k_batched<64, 5, 6, false, true, 1, true>);
-    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, true, 0, true>);  // 8 to 11
+    default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, true, 0, true>);  // 8 to 11, 20
   }
 }
 
