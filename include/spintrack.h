@@ -158,7 +158,10 @@ size_t st_param_table_bytes(const st_ctx *ctx);
 int st_set_launch_config(st_ctx *ctx, const st_launch_config *cfg);
 int st_get_launch_config(const st_ctx *ctx, st_launch_config *cfg);
 /* Number of persistent-kernel variants (valid st_launch_config.variant
- * values are 0 .. count-1) and the name of one, for external tuners. */
+ * values are 0 .. count-1) and the name of one, for external tuners.  The
+ * autotuner offers the flattened ("flat_*") and trajectory-ahead ("ahead_*")
+ * variants; the warp-specialised ("split_*") and three-lanes-per-particle
+ * ("tpp3_*") ones run only when chosen here. */
 int st_launch_variant_count(void);
 const char *st_launch_variant_name(int variant);
 /* Device time budget for each following run call, in seconds (0 = none).

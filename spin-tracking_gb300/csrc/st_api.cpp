@@ -1825,6 +1825,10 @@ int autotune(st_ctx* c) {
   // the variant): on every workload measured, fewer resident blocks lost.
   for (int v = 0; v < nv; ++v) {
     if (st::persistent_max_blocks_per_sm(v, ext) <= 0) continue;  // not built for this kind of run
+    // The warp-specialised and three-lane variants were slower on every
+    // workload measured, and a short sample can favour them: only an explicit
+    // st_set_launch_config selects them.
+    if (st::persistent_variant_family(v) >= 2) continue;
     const int maxb = std::max(1, st::persistent_max_blocks_per_sm(v, ext));
     {
       st_launch_config cfg{0, maxb, v};

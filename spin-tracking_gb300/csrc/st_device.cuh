@@ -134,6 +134,17 @@ __device__ __forceinline__ uint64_t rng_next(Rng& r) {
 // top 53 bits scaled by 2^-53 (exact), src/particle.cpp:72-83
 __device__ __forceinline__ double rng_uniform(Rng& r) { return xmul((double)(rng_next(r) >> 11), 0x1.0p-53); }
 
+// The uniform pairs of the Marsaglia polar method until 0 < s = u^2 + v^2 < 1,
+// and the factor sqrt(-2 log s / s) from log s.
+__device__ __forceinline__ void marsaglia_draw(Rng& r, double& u, double& v, double& s) {
+  do {
+    u = xadd(xmul(rng_uniform(r), 2.0), -1.0);
+    v = xadd(xmul(rng_uniform(r), 2.0), -1.0);
+    s = xadd(xmul(u, u), xmul(v, v));
+  } while (s >= 1.0 || s == 0.0);
+}
+__device__ __forceinline__ double marsaglia_factor(double s, double log_s) { return xsqrt(xdiv(xmul(-2.0, log_s), s)); }
+
 // Marsaglia polar normal with cached spare (src/particle.cpp:89-107).
 __device__ __forceinline__ double rng_normal(Rng& r, double mean, double sd) {
   if (r.has) {
@@ -141,15 +152,11 @@ __device__ __forceinline__ double rng_normal(Rng& r, double mean, double sd) {
     return xadd(xmul(r.spare, sd), mean);
   }
   double u, v, s;
-  do {
-    u = xadd(xmul(rng_uniform(r), 2.0), -1.0);
-    v = xadd(xmul(rng_uniform(r), 2.0), -1.0);
-    s = xadd(xmul(u, u), xmul(v, v));
-  } while (s >= 1.0 || s == 0.0);
-  s = xsqrt(xdiv(xmul(-2.0, traj_log(s)), s));
-  r.spare = xmul(v, s);
+  marsaglia_draw(r, u, v, s);
+  const double f = marsaglia_factor(s, traj_log(s));
+  r.spare = xmul(v, f);
   r.has = true;
-  return xadd(mean, xmul(xmul(sd, u), s));
+  return xadd(mean, xmul(xmul(sd, u), f));
 }
 __device__ __forceinline__ double rng_exponential(Rng& r, double tc) {
   return xmul(-tc, traj_log(xsub(1.0, rng_uniform(r))));
@@ -271,12 +278,18 @@ struct SegStart {
   double t, px, py, pz, vx, vy, vz;
 };
 
-// A cosine-law diffuse reflection whose draws were taken but whose velocity
-// is not yet computed (traj_event<true>).
-struct DiffuseDefer {
-  double su, theta, speed;  // sqrt(u1), 2 pi u2, |v| at the wall
+// A trajectory event whose draws were taken but whose logarithms, sines and
+// cosines are not yet computed (traj_event<true>): a cosine-law diffuse
+// reflection, or a gas collision with a Maxwell-Boltzmann velocity redraw.
+//   reflection: x[0] = sqrt(u1), x[1] = theta = 2 pi u2, x[2] = |v| at the wall
+//   gas:        x[0] = 1 - u of the gas clock's exponential draw, then the
+//               Marsaglia pairs drawn for the three velocity normals, (u, v, s)
+//               in x[1..3] and x[4..6]: one pair when the first normal is the
+//               cached spare (spare_first), two otherwise
+struct EventDefer {
+  double x[7];
   char wall;
-  bool pending;
+  bool pending, gas, spare_first;
 };
 
 // New velocity of a cosine-law diffuse reflection off wall w from the sin and
@@ -321,62 +334,137 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
   return p;
 }
 
-// The deferred diffuse reflections of a warp, lanes `pend`, computed by all
-// 32 lanes together (the warp must be converged).  A reflection needs the sin
-// and cos of two angles: the argument of its acos Newton step and theta.
-// Those 2 popc(pend) evaluations are dealt out one per lane per pass (one pass
-// for up to 16 reflections) instead of two after each other on each pending
-// lane; each pending lane then finishes its own reflection from the shuffled
-// results.  The arithmetic of every evaluation is diffuse_velocity's, so the
-// velocities are the same bit for bit.
-__device__ __forceinline__ void diffuse_velocity_warp(PState& p, DiffuseDefer& dd, unsigned pend, int lane) {
+// The rest of a deferred gas collision from the logarithms of its draws
+// (log_a of the gas clock's 1 - u, log_s0 and log_s1 of the Marsaglia pairs):
+// the gas clock as rng_exponential advances it, the three normals and the
+// cached spare as three rng_normal calls leave them, the Maxwell-Boltzmann
+// velocity (src/particle.cpp:117-119, 89-111, 373-380).
+__device__ __forceinline__ void gas_finish(PState& p, const SetParams& P, const EventDefer& dd, double log_a,
+                                           double log_s0, double log_s1) {
+  p.next_gas = xadd(p.next_gas, xmul(-P.tc, log_a));
+  const double f0 = marsaglia_factor(dd.x[3], log_s0);
+  const double pair0 = xadd(0.0, xmul(xmul(1.0, dd.x[1]), f0));
+  const double spare0 = xmul(dd.x[2], f0);
+  double n1, n2, n3;
+  if (dd.spare_first) {
+    n1 = xadd(xmul(p.rng.spare, 1.0), 0.0);
+    n2 = pair0;
+    n3 = xadd(xmul(spare0, 1.0), 0.0);
+    p.rng.spare = spare0;
+  } else {
+    const double f1 = marsaglia_factor(dd.x[6], log_s1);
+    n1 = pair0;
+    n2 = xadd(xmul(spare0, 1.0), 0.0);
+    n3 = xadd(0.0, xmul(xmul(1.0, dd.x[4]), f1));
+    p.rng.spare = xmul(dd.x[5], f1);
+  }
+  p.vx = xmul(n1, P.sqrtKT_m);
+  p.vy = xmul(n2, P.sqrtKT_m);
+  p.vz = xmul(n3, P.sqrtKT_m);
+}
+
+// The deferred events of a warp, lanes `pend`, computed by all 32 lanes
+// together (the warp must be converged).  A diffuse reflection needs the sin
+// and cos of two angles (the argument of its acos Newton step and theta), a
+// gas collision the logarithms of up to three of its draws.  Those
+// evaluations are dealt out one per lane per pass (one pass for up to 16
+// reflections, another for up to 10 gas collisions) instead of running one
+// after the other on each pending lane; each pending lane then finishes its
+// own event from the shuffled results.  Every value is computed by the code of
+// the per-lane path (diffuse_velocity, rng_exponential, rng_normal), so the
+// results are the same bit for bit.
+template <bool GAS>
+__device__ __forceinline__ void deferred_events_warp(PState& p, const SetParams& P, EventDefer& dd, unsigned pend,
+                                                     int lane) {
 #if ST_TRAJ_CORRECTLY_ROUNDED
   const unsigned FULL = 0xffffffffu;
-  const int np = __popc(pend);
-  const bool mine = dd.pending;
-  const double x = dd.su;
-  double y0 = 0.0, arg_a = 0.0;
-  if (mine) {
-    y0 = acos(x);
-    arg_a = x < 1.0 ? crm::acos_newton_arg(x, y0) : 0.0;  // NaN and 1 use none
-  }
-  const int rank = __popc(pend & ((1u << lane) - 1u));
-  crm::DD sa{0.0, 0.0}, ca{1.0, 0.0}, st{0.0, 0.0}, ct{1.0, 0.0};
-  for (int base = 0; base < 2 * np; base += 32) {
-    // job j = base + lane: the Newton argument of pending lane j (j < np) or
-    // the theta of pending lane j - np
-    const int j = base + lane;
-    const int src = nth_set_bit(pend, min(j < np ? j : j - np, np - 1));
-    const double a1 = __shfl_sync(FULL, arg_a, src), a2 = __shfl_sync(FULL, dd.theta, src);
-    crm::DD sn, cs;
-    crm::sincos_dd(j < np ? a1 : a2, sn, cs);
-    // pending lane of rank r takes jobs r and np + r
-    const int ja = rank - base, jb = np + rank - base;
-    const double v0 = __shfl_sync(FULL, sn.hi, ja & 31), v1 = __shfl_sync(FULL, sn.lo, ja & 31);
-    const double v2 = __shfl_sync(FULL, cs.hi, ja & 31), v3 = __shfl_sync(FULL, cs.lo, ja & 31);
-    const double w0 = __shfl_sync(FULL, sn.hi, jb & 31), w1 = __shfl_sync(FULL, sn.lo, jb & 31);
-    const double w2 = __shfl_sync(FULL, cs.hi, jb & 31), w3 = __shfl_sync(FULL, cs.lo, jb & 31);
-    if (ja >= 0 && ja < 32) {
-      sa = {v0, v1};
-      ca = {v2, v3};
+  const unsigned below = (1u << lane) - 1u;
+  const unsigned refl = GAS ? __ballot_sync(FULL, dd.pending && !dd.gas) : pend;
+  if (refl) {
+    const int np = __popc(refl);
+    const bool mine = dd.pending && !dd.gas;
+    const double x = dd.x[0];
+    double y0 = 0.0, arg_a = 0.0;
+    if (mine) {
+      y0 = acos(x);
+      arg_a = x < 1.0 ? crm::acos_newton_arg(x, y0) : 0.0;  // NaN and 1 use none
     }
-    if (jb >= 0 && jb < 32) {
-      st = {w0, w1};
-      ct = {w2, w3};
+    const int rank = __popc(refl & below);
+    crm::DD sa{0.0, 0.0}, ca{1.0, 0.0}, st{0.0, 0.0}, ct{1.0, 0.0};
+    for (int base = 0; base < 2 * np; base += 32) {
+      // job j = base + lane: the Newton argument of reflection j (j < np) or
+      // the theta of reflection j - np
+      const int j = base + lane;
+      const int src = nth_set_bit(refl, min(j < np ? j : j - np, np - 1));
+      const double a1 = __shfl_sync(FULL, arg_a, src), a2 = __shfl_sync(FULL, dd.x[1], src);
+      crm::DD sn, cs;
+      crm::sincos_dd(j < np ? a1 : a2, sn, cs);
+      // the reflection of rank r takes jobs r and np + r
+      const int ja = rank - base, jb = np + rank - base;
+      const double v0 = __shfl_sync(FULL, sn.hi, ja & 31), v1 = __shfl_sync(FULL, sn.lo, ja & 31);
+      const double v2 = __shfl_sync(FULL, cs.hi, ja & 31), v3 = __shfl_sync(FULL, cs.lo, ja & 31);
+      const double w0 = __shfl_sync(FULL, sn.hi, jb & 31), w1 = __shfl_sync(FULL, sn.lo, jb & 31);
+      const double w2 = __shfl_sync(FULL, cs.hi, jb & 31), w3 = __shfl_sync(FULL, cs.lo, jb & 31);
+      if (ja >= 0 && ja < 32) {
+        sa = {v0, v1};
+        ca = {v2, v3};
+      }
+      if (jb >= 0 && jb < 32) {
+        st = {w0, w1};
+        ct = {w2, w3};
+      }
+    }
+    if (mine) {
+      double phi, sp, cp;
+      if (!crm::acos_sincos_given(x, y0, sa, ca, phi, sp, cp)) crm::cr_acos_sincos(x, phi, sp, cp);
+      double stt = st.hi, ctt = ct.hi;
+      if (!(crm::trig_sure(st) && crm::trig_sure(ct))) crm::sincos_accurate(dd.x[1], stt, ctt);
+      diffuse_apply(p, sp, cp, stt, ctt, dd.x[2], dd.wall);
+      dd.pending = false;
     }
   }
-  if (mine) {
-    double phi, sp, cp;
-    if (!crm::acos_sincos_given(x, y0, sa, ca, phi, sp, cp)) crm::cr_acos_sincos(x, phi, sp, cp);
-    double stt = st.hi, ctt = ct.hi;
-    if (!(crm::trig_sure(st) && crm::trig_sure(ct))) crm::sincos_accurate(dd.theta, stt, ctt);
-    diffuse_apply(p, sp, cp, stt, ctt, dd.speed, dd.wall);
-    dd.pending = false;
+  if (GAS) {
+    const unsigned gm = pend & ~refl;
+    if (gm) {
+      const int ng = __popc(gm);
+      const bool mine = dd.pending && dd.gas;
+      const double third = dd.spare_first ? 1.0 : dd.x[6];  // log 1 = 0 fills the unused job
+      const int rank = __popc(gm & below);
+      double l0 = 0.0, l1 = 0.0, l2 = 0.0;
+      for (int base = 0; base < 3 * ng; base += 32) {
+        // job j = base + lane: draw j % 3 (1 - u, s of pair 0, s of pair 1)
+        // of gas collision j / 3
+        const int j = base + lane;
+        const int q = min(j / 3, ng - 1), k = j - 3 * (j / 3);
+        const int src = nth_set_bit(gm, q);
+        const double a0 = __shfl_sync(FULL, dd.x[0], src), a1 = __shfl_sync(FULL, dd.x[3], src);
+        const double a2 = __shfl_sync(FULL, third, src);
+        const double arg = k == 0 ? a0 : (k == 1 ? a1 : a2);
+        double y;
+        if (!crm::cr_log_fast(arg, y)) y = crm::log_accurate(arg);
+        // the collision of rank r takes jobs 3r, 3r + 1, 3r + 2
+        const int jr = 3 * rank - base;
+        const double r0 = __shfl_sync(FULL, y, jr & 31), r1 = __shfl_sync(FULL, y, (jr + 1) & 31);
+        const double r2 = __shfl_sync(FULL, y, (jr + 2) & 31);
+        if (jr >= 0 && jr < 32) l0 = r0;
+        if (jr + 1 >= 0 && jr + 1 < 32) l1 = r1;
+        if (jr + 2 >= 0 && jr + 2 < 32) l2 = r2;
+      }
+      if (mine) {
+        gas_finish(p, P, dd, l0, l1, l2);
+        dd.pending = false;
+        dd.gas = false;
+      }
+    }
   }
 #else
   if (dd.pending) {
-    diffuse_velocity(p, dd.su, dd.theta, dd.speed, dd.wall);
+    if (GAS && dd.gas)
+      gas_finish(p, P, dd, traj_log(dd.x[0]), traj_log(dd.x[3]), dd.spare_first ? 0.0 : traj_log(dd.x[6]));
+    else
+      diffuse_velocity(p, dd.x[0], dd.x[1], dd.x[2], dd.wall);
     dd.pending = false;
+    dd.gas = false;
   }
 #endif
 }
@@ -386,13 +474,18 @@ __device__ __forceinline__ void diffuse_velocity_warp(PState& p, DiffuseDefer& d
 // end tf was reached).  Fills the segment start.
 //
 // DEFER: a diffuse reflection's draws are taken here (the RNG sequence is
-// unchanged) but its velocity is left to diffuse_velocity, called later by the
-// trajectory-ahead kernel for many lanes at once.  The sanity check then sees
-// the velocity before the reflection; that gives the same outcome: the
+// unchanged) but its velocity is left to deferred_events_warp, called later by
+// the trajectory-ahead kernel for many lanes at once.  The sanity check then
+// sees the velocity before the reflection; that gives the same outcome: the
 // reflected velocity is |v| times sines and cosines that are finite and, for
 // the draws possible here, non-zero except cos(phi) at u1 = 0, so it is NaN
 // or infinite only when the velocity before it already was, which fails the
-// same check (NaN) or the position check before it (infinite).
+// same check (NaN) or the position check before it (infinite).  A gas
+// collision with a Maxwell-Boltzmann redraw is deferred the same way: its
+// uniform draws are taken here in the reference's order, the logarithms (of
+// the gas clock and of the Marsaglia pairs) later.  Its new velocity is the
+// product of finite normals and a finite sqrt(kT/m), so the NaN check gives the
+// outcome it gives on the velocity before the collision (which it also tests).
 //
 // GAS = false: compiled for launches in which no parameter set has gas
 // collisions.  Their gas clock is DBL_MAX and never moves, so the gas
@@ -401,7 +494,7 @@ __device__ __forceinline__ void diffuse_velocity_warp(PState& p, DiffuseDefer& d
 // limit either way.
 template <bool DEFER = false, bool GAS = true>
 __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double tf, SegStart& s0,
-                                           DiffuseDefer* dd = nullptr) {
+                                           EventDefer* dd = nullptr) {
   const double G = kGravity;
   const double hLx = P.Lx / 2.0, hLy = P.Ly / 2.0, hLz = P.Lz / 2.0;
   double dtx, dty, dtz;
@@ -500,7 +593,12 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
     if (gas_next) {
       p.coll = 'G';
       p.n_coll += 1;
-      p.next_gas = xadd(p.next_gas, rng_exponential(p.rng, P.tc));
+      if (DEFER && P.dist == 'M' && isfinite(P.sqrtKT_m)) {
+        dd->x[0] = xsub(1.0, rng_uniform(p.rng));  // rng_exponential's draw; its log later
+        dd->gas = true;
+      } else {
+        p.next_gas = xadd(p.next_gas, rng_exponential(p.rng, P.tc));
+      }
     } else {
       p.n_bounce += 1;
       p.coll = 'W';
@@ -543,10 +641,11 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
       const double theta = xmul(xmul(rng_uniform(p.rng), 2.0), 3.141592653589793);
       if (w == 'x' || w == 'y' || w == 'z') {
         if (DEFER) {
-          dd->su = su;
-          dd->theta = theta;
-          dd->speed = speed;
+          dd->x[0] = su;
+          dd->x[1] = theta;
+          dd->x[2] = speed;
           dd->wall = w;
+          dd->gas = false;
           dd->pending = true;
         } else {
           diffuse_velocity(p, su, theta, speed, w);
@@ -560,7 +659,16 @@ __device__ __forceinline__ bool traj_event(PState& p, const SetParams& P, double
       if (sz) p.vz = -p.vz;
     }
   } else if (GAS && p.coll == 'G') {
-    if (P.dist == 'M') {
+    if (DEFER && dd->gas) {
+      // the three normals' uniform draws now, in rng_normal's order: the first
+      // normal is the cached spare or opens pair 0, whose spare is the second;
+      // the third opens pair 1 (its spare stays cached) or is pair 0's spare
+      dd->spare_first = p.rng.has;
+      marsaglia_draw(p.rng, dd->x[1], dd->x[2], dd->x[3]);
+      if (!dd->spare_first) marsaglia_draw(p.rng, dd->x[4], dd->x[5], dd->x[6]);
+      p.rng.has = !dd->spare_first;
+      dd->pending = true;
+    } else if (P.dist == 'M') {
       p.vx = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);
       p.vy = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);
       p.vz = xmul(rng_normal(p.rng, 0.0, 1.0), P.sqrtKT_m);

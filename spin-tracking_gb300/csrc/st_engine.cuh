@@ -403,7 +403,7 @@ __device__ __forceinline__ DeviceState state_slot(const DeviceState& b, int64_t 
 
 template <int BLOCK, bool TAPE, bool GAS, bool EXT>
 __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, double tf, double* qd, int* qf,
-                                               int slot, int tid, bool& blocked, DiffuseDefer& dd, const TapeArgs& ta,
+                                               int slot, int tid, bool& blocked, EventDefer& dd, const TapeArgs& ta,
                                                TapeCursor& tc) {
   SegStart s0;
   const uint64_t nb = tp.n_bounce, nc = tp.n_coll;
@@ -430,10 +430,11 @@ __device__ __forceinline__ void produce_record(PState& tp, const SetParams& P, d
 
 enum BatchedMode { B_FETCH = 0, B_NEED = 1, B_SEG = 2, B_WEND = 3, B_DONE = 4 };
 
-// Diffuse reflections are deferred (traj_event<true>): a lane with one pending
-// produces no further records until the warp computes the pending
-// reflections together, when defer_k lanes have one, or one of them is about
-// to run dry or has reached its window end.
+// Diffuse reflections and Maxwell-Boltzmann gas collisions are deferred
+// (traj_event<true>): a lane with one pending produces no further records
+// until the warp computes the pending events together (deferred_events_warp),
+// when defer_k lanes have one, or one of them is about to run dry or has
+// reached its window end.
 // TAPE: also write the adjoint tape (steps and segments of every particle)
 // and state checkpoints at every ta.ckpt_every-th window end.
 // GAS = false: the instantiation for launches without gas collisions.
@@ -466,8 +467,9 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   TapeCursor tc;
   tape_open(tc);
-  DiffuseDefer dd;
+  EventDefer dd;
   dd.pending = false;
+  dd.gas = false;
   while (true) {
     // ---- A: spin-side boundaries of this lane (pop records, window ends, fetch)
     bool starved = false;
@@ -575,7 +577,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     const unsigned defer_m = __ballot_sync(FULL, dd.pending);
     if (defer_m != 0u &&
         (__popc(defer_m) >= defer_k || __any_sync(FULL, dd.pending && (starved || qcount <= 1 || mode == B_WEND))))
-      diffuse_velocity_warp(tp, dd, defer_m, tid & 31);
+      deferred_events_warp<GAS>(tp, *P, dd, defer_m, tid & 31);
     bool prod = (mode == B_NEED || mode == B_SEG) && !blocked && qcount < QCAP && !dd.pending;
     unsigned pm = __ballot_sync(FULL, prod);
     if (starved_m != 0u || __popc(pm) >= topup_start) {

@@ -207,6 +207,8 @@ int set_last_error(int code, const char* msg);
 int persistent_max_blocks_per_sm(int variant, int kind);
 int persistent_prepare(int variant);
 int persistent_variant_block(int variant);
+// 0 flattened, 1 trajectory-ahead, 2 warp-specialised, 3 three lanes per particle
+int persistent_variant_family(int variant);
 const char* persistent_variant_name(int variant);
 
 }  // namespace st

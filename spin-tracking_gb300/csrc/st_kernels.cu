@@ -221,6 +221,7 @@ constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int persistent_variant_count() { return kNumVariants; }
 int persistent_variant_block(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].block : 0; }
+int persistent_variant_family(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].family : -1; }
 const char* persistent_variant_name(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "?"; }
 
 template <bool GAS>
