@@ -170,13 +170,9 @@ static __device__ __noinline__ double log_accurate(double x) {
 
 // Natural logarithm of a positive normal double: the correctly rounded y and
 // true, or false when the fast value's rounding is uncertain; log(1) = 0.
-static __device__ __noinline__ bool cr_log_fast(double x, double& y) {
-  const LogReduced r = log_reduce(x);
+// The fast double-double log of x from its reduction (x != 1).
+__device__ __forceinline__ DD log_fast_dd(const LogReduced& r) {
   const DD t = r.t;
-  if (t.hi == 0.0 && r.e == 0 && r.j >= 31 && r.j <= 32) {  // x = 1
-    y = 0.0;
-    return true;
-  }
   // log1p(t) = t - t^2/2 + t^3/3 - t^4/4 + ... + t^13/13
   const double z = t.hi;
   double tail = 1.0 / 13.0;
@@ -196,7 +192,18 @@ static __device__ __noinline__ bool cr_log_fast(double x, double& y) {
   DD l = dd_add(t, {-0.5 * t2.hi, -0.5 * t2.lo});
   l = dd_add(l, dd_mul(t3, {kThirdHi, kThirdLo}));
   l = dd_add_d(l, tail);
-  const DD s = log_assemble(r, l);
+  return log_assemble(r, l);
+}
+__device__ __forceinline__ bool log_is_one(const LogReduced& r) {
+  return r.t.hi == 0.0 && r.e == 0 && r.j >= 31 && r.j <= 32;
+}
+static __device__ __noinline__ bool cr_log_fast(double x, double& y) {
+  const LogReduced r = log_reduce(x);
+  if (log_is_one(r)) {  // x = 1
+    y = 0.0;
+    return true;
+  }
+  const DD s = log_fast_dd(r);
   y = s.hi;
   return rounds_surely(s.hi, s.lo, rel_err(s.hi, kLogFastErr));
 }
