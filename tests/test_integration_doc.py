@@ -1,6 +1,7 @@
-"""The C++ binding shown in INTEGRATION.md (the reference's `particle` class
-re-implemented over the C ABI) compiles and links against the library, with
-stand-ins for the reference's `coords`, `options` and `Logger` types."""
+"""The C++ binding of the repository's integration guide (the reference's
+`particle` class re-implemented over the C ABI) compiles and links against the
+library, with stand-ins for the reference's `coords`, `options` and `Logger`
+types."""
 from __future__ import annotations
 
 import re
