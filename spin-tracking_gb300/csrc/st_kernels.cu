@@ -216,6 +216,8 @@ static const Variant kVariants[] = {
     {2, 384, 1, 8, 0, 0, 0, 0, "split_c8p4_q8_r184_136", 8, 4, 184, 136},
     {3, 128, 2, 0, 0, 0, 0, 0, "tpp3_b128_m2"},    {3, 128, 3, 0, 0, 0, 0, 0, "tpp3_b128_m3"},
     {1, 128, 1, 6, 16, 12, 16, 0, "ahead_b128_q6_t16_d16"}, {1, 64, 2, 8, 24, 16, 16, 0, "ahead_b64_q8_t24_d16"},
+    {1, 64, 2, 12, 24, 16, 12, 0, "ahead_b64_q12_t24_d12"}, {1, 64, 2, 12, 28, 20, 16, 0, "ahead_b64_q12_t28_d16"},
+    {1, 64, 2, 12, 20, 12, 12, 0, "ahead_b64_q12_t20_d12"}, {1, 64, 2, 12, 16, 8, 12, 0, "ahead_b64_q12_t16_d12"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -252,6 +254,10 @@ static const void* variant_fn_g(int v) {
     case 17:
     case 18: return nullptr;  // the three-lane step assumes the default field hooks
 #endif
+    case 21:
+    case 22:
+    case 23:
+    case 24: return reinterpret_cast<const void*>(&k_batched<64, 2, 12, false, GAS, 0, false>);
     default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, GAS, 0, false>);  // 8 to 11, 20
   }
 }

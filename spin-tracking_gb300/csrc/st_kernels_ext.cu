@@ -22,6 +22,10 @@ const void* variant_fn_ext(int v) {
     case 7: return reinterpret_cast<const void*>(&k_batched<128, 2, 4, false, true, 0, true>);
     case 12: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, true, 1, true>);
     case 13: return reinterpret_cast<const void*>(&k_batched<64, 5, 6, false, true, 1, true>);
+    case 21:
+    case 22:
+    case 23:
+    case 24: return reinterpret_cast<const void*>(&k_batched<64, 2, 12, false, true, 0, true>);
     default: return reinterpret_cast<const void*>(&k_batched<64, 2, 8, false, true, 0, true>);  // 8 to 11, 20
   }
 }
