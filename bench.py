@@ -633,12 +633,12 @@ def run_ours(args, world, rank, local):
                                 "flops": flops, "kernel_ms": kernel_s * 1e3}}
     # DRAM bytes of one launch, from an ncu capture of dram__bytes_read.sum + dram__bytes_write.sum
     # (one pass) of this kernel on this workload at its full size, 1,048,576 particles and two
-    # windows: 282.23 MB read (the state, once) + 460.47 MB written (the state and a snapshot block
-    # at each window end), 708 B per particle per two windows; other sizes scale by particles and
+    # windows: 279.85 MB read (the state, once) + 453.40 MB written (the state and a snapshot block
+    # at each window end), 699 B per particle per two windows; other sizes scale by particles and
     # windows (every particle's state and snapshot cross DRAM once per window end).
-    roof["traffic"] = 742.7e6 * (n / 1048576.0) * (nwin / 2.0)
+    roof["traffic"] = 733.3e6 * (n / 1048576.0) * (nwin / 2.0)
     roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel on the full "
-                              "workload (1,048,576 particles, 2 windows: 742.7 MB), scaled to this launch")
+                              "workload (1,048,576 particles, 2 windows: 733.3 MB), scaled to this launch")
 
     # ---- plain one-thread-per-particle kernel on the same workload (1 step)
     plain = None
