@@ -467,9 +467,13 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   TapeCursor tc;
   tape_open(tc);
-  EventDefer dd;
+  EventDefer dd;  // every field set: the warp's flush shuffles them from every lane
+#pragma unroll
+  for (int k = 0; k < 7; ++k) dd.x[k] = 0.0;
+  dd.wall = 'x';
   dd.pending = false;
   dd.gas = false;
+  dd.spare_first = false;
   while (true) {
     // ---- A: spin-side boundaries of this lane (pop records, window ends, fetch)
     bool starved = false;
